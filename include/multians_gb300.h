@@ -1,0 +1,111 @@
+/*
+ * multians_gb300 -- C ABI of the GB300 (sm_103a) MULTIANS tANS decoder.
+ *
+ * Plain pointers and sizes only.  Device pointers are CUDA device memory of
+ * the current device; `stream` is a cudaStream_t passed as void* (NULL =
+ * legacy default stream).  Every entry point returns a mans_status code.
+ *
+ * Data formats are the reference's own:
+ *   stream units  uint32, in CUHDInputBuffer order (the encoder's units
+ *                 reversed; src/multians_input_buffer.cc:29); units past
+ *                 n_units are treated as the zero padding
+ *                 (src/multians_input_buffer.cc:23)
+ *   table         L uint32 words, each a CUHDCodetableItem
+ *                 {u16 next_state, u8 symbol, u8 min_num_bits}
+ *                 (include/cuhd_codetable.h:20-24)
+ *   output        n_out uint8 symbols in decode order, i.e. reversed like
+ *                 the reference GPU decoder's output (src/main.cc:119-123)
+ */
+#ifndef MULTIANS_GB300_H_
+#define MULTIANS_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MANS_OK = 0,
+    MANS_ERR_ARG = 1,          /* bad argument (sizes, L, first_state ...) */
+    MANS_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    MANS_ERR_AUX_SMALL = 3,    /* decoder memory smaller than needed */
+    MANS_ERR_TABLE = 4,        /* table entry outside the decodable form */
+    MANS_ERR_SYNC = 5,         /* a sync walk ran past its slots */
+    MANS_ERR_NOMEM = 6,        /* allocation failed */
+    MANS_ERR_BUSY = 7,         /* serving queue full / budget exhausted */
+    MANS_ERR_NOT_FOUND = 8     /* unknown request / handle */
+} mans_status;
+
+/* Device-side status bits (mans_aux_status). */
+#define MANS_DEV_BAD_TABLE      0x1u   /* invalid table entry seen */
+#define MANS_DEV_SYNC_OVERFLOW  0x2u   /* a walk needed more slots */
+#define MANS_DEV_DEGENERATE     0x4u   /* single-symbol table: filled */
+#define MANS_DEV_COUNT_MISMATCH 0x8u   /* final pass disagreed with scan */
+
+/* Launch geometry of one decode.  Zero fields are chosen by the built-in
+ * autotuner from (L, units, output size). */
+typedef struct {
+    uint32_t block_units;     /* units per output block (final pass) */
+    uint32_t region_blocks;   /* blocks per sync region */
+    uint32_t walk_slots;      /* regions a sync walk may cross */
+    uint32_t threads;         /* threads per CTA */
+} mans_cfg;
+
+/* Fills `out` with the geometry the decoder uses for this call. */
+int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
+              mans_cfg* out);
+
+/* Bytes of decoder memory ("aux") a decode with this geometry needs.
+ * Replaces CUHDGPUDecoderMemory's sizing by (num_units, subsequence size,
+ * threads) in src/multians_gpu_decoder_memory.cc:13-50. */
+size_t mans_aux_size(size_t n_units, const mans_cfg* cfg);
+
+/* Worst-case aux bytes over every geometry mans_plan can pick for n_units
+ * units (what CUHDGPUDecoderMemory::allocate reserves). */
+size_t mans_aux_size_max(size_t n_units);
+
+/* Decodes one stream; asynchronous on `stream`.  Replaces
+ * cuhd::CUHDGPUDecoder::decode (include/cuhd_gpu_decoder.h:24-35,
+ * src/multians_gpu_decoder.cu:575-687): same inputs (units, table, initial
+ * state and bit, number of states), same output.  Allocates nothing.
+ * cfg may be NULL (autotuned).  Argument errors return immediately; data
+ * errors are reported through mans_aux_status. */
+int mans_decode(const uint32_t* d_units, size_t n_units,
+                uint8_t* d_out, size_t n_out,
+                const uint32_t* d_table, uint32_t L,
+                uint32_t first_state, uint32_t first_bit,
+                void* d_aux, size_t aux_bytes,
+                const mans_cfg* cfg, void* stream);
+
+/* Waits for `stream` and returns the device status bits of the last decode
+ * that used d_aux (0 = clean). */
+int mans_aux_status(const void* d_aux, void* stream, uint32_t* status_out);
+
+/* Synchronous decode: mans_decode, then the status check; on a sync-walk
+ * overflow it re-plans with four times longer regions and decodes again.
+ * hint may be NULL. */
+int mans_decode_sync(const uint32_t* d_units, size_t n_units,
+                     uint8_t* d_out, size_t n_out,
+                     const uint32_t* d_table, uint32_t L,
+                     uint32_t first_state, uint32_t first_bit,
+                     void* d_aux, size_t aux_bytes, const mans_cfg* hint,
+                     void* stream, uint32_t* status_out);
+
+/* Host-side table check: 0 if every entry decodes inside [L, 2L) and
+ * zero-bit entries strictly decrease the state, 1 if the table holds a
+ * single symbol (all entries are zero-bit self loops), -1 otherwise. */
+int mans_table_check(const uint32_t* h_table, uint32_t L);
+
+/* Number of kernels launched by the last decode on this thread. */
+uint32_t mans_last_launch_count(void);
+
+/* Library version string. */
+const char* mans_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MULTIANS_GB300_H_ */

@@ -1,0 +1,118 @@
+"""ctypes loader of libmultians_gb300.so and the C ABI signatures
+(include/multians_gb300.h)."""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libmultians_gb300.so")
+
+DEV_BAD_TABLE = 0x1
+DEV_SYNC_OVERFLOW = 0x2
+DEV_DEGENERATE = 0x4
+DEV_COUNT_MISMATCH = 0x8
+
+
+class Status(enum.IntEnum):
+    OK = 0
+    ERR_ARG = 1
+    ERR_CUDA = 2
+    ERR_AUX_SMALL = 3
+    ERR_TABLE = 4
+    ERR_SYNC = 5
+    ERR_NOMEM = 6
+    ERR_BUSY = 7
+    ERR_NOT_FOUND = 8
+
+
+class MansError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        try:
+            name = Status(code).name
+        except ValueError:
+            name = f"status {code}"
+        super().__init__(f"{what}: {name}" if what else name)
+        self.code = code
+
+
+class Cfg(ctypes.Structure):
+    _fields_ = [("block_units", ctypes.c_uint32), ("region_blocks", ctypes.c_uint32),
+                ("walk_slots", ctypes.c_uint32), ("threads", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+_vp = ctypes.c_void_p
+_sz = ctypes.c_size_t
+_u32 = ctypes.c_uint32
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+
+# (name, restype, argtypes) of every exported entry point
+SIGNATURES = {
+    "mans_version": (ctypes.c_char_p, []),
+    "mans_last_launch_count": (_u32, []),
+    "mans_plan": (ctypes.c_int, [_sz, _sz, _u32, ctypes.POINTER(Cfg), ctypes.POINTER(Cfg)]),
+    "mans_aux_size": (_sz, [_sz, ctypes.POINTER(Cfg)]),
+    "mans_aux_size_max": (_sz, [_sz]),
+    "mans_table_check": (ctypes.c_int, [_u32p, _u32]),
+    "mans_decode": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _u32, _u32, _u32, _vp, _sz,
+                                   ctypes.POINTER(Cfg), _vp]),
+    "mans_aux_status": (ctypes.c_int, [_vp, _vp, _u32p]),
+    "mans_decode_sync": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _u32, _u32, _u32, _vp, _sz,
+                                        ctypes.POINTER(Cfg), _vp, _u32p]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded native library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc != 0:
+        raise MansError(rc, what)
+
+
+def version() -> str:
+    return lib().mans_version().decode()
+
+
+def plan(n_units: int, n_out: int, L: int, hint: dict | None = None) -> dict:
+    h = Cfg(**(hint or {}))
+    out = Cfg()
+    check(lib().mans_plan(n_units, n_out, L, ctypes.byref(h), ctypes.byref(out)), "mans_plan")
+    return out.as_dict()
+
+
+def aux_size(n_units: int, cfg: dict) -> int:
+    c = Cfg(**cfg)
+    return int(lib().mans_aux_size(n_units, ctypes.byref(c)))
+
+
+def aux_size_max(n_units: int) -> int:
+    return int(lib().mans_aux_size_max(n_units))
+
+
+def table_check(table) -> int:
+    """0 = decodable, 1 = single-symbol table, -1 = invalid (host check)."""
+    import numpy as np
+    t = np.ascontiguousarray(table, dtype=np.uint32)
+    return int(lib().mans_table_check(t.ctypes.data_as(_u32p), t.size))

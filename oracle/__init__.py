@@ -1,0 +1,5 @@
+"""CPU oracle for the MULTIANS decode path (test infrastructure only).
+
+Loaded by tests/, by ``__graft_entry__.smoke()`` as the checker and by
+``bench.py`` for its CPU baseline.  The product package never imports it.
+"""

@@ -1,0 +1,83 @@
+"""CPU tests of the native boundary: the library loads (no GPU needed) and
+exports every entry point that include/*.h declares; host-side planning and
+table checks behave."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
+
+
+def _declared_c_symbols():
+    names = set()
+    for f in os.listdir(INCLUDE):
+        if not f.endswith(".h"):
+            continue
+        text = open(os.path.join(INCLUDE, f)).read()
+        if 'extern "C"' not in text:
+            continue
+        for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(mans_\w+)\s*\(", text, re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_entry_points():
+    names = _declared_c_symbols()
+    assert "mans_decode" in names and "mans_aux_size" in names
+
+
+def test_library_exports_declared_symbols(mg):
+    lib = mg.lib()
+    out = subprocess.run(["nm", "-D", "--defined-only", mg.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if ln.strip()}
+    missing = [n for n in _declared_c_symbols() if n not in exported]
+    assert not missing, missing
+    for n in _declared_c_symbols():
+        assert hasattr(lib, n)
+
+
+def test_version(mg):
+    assert mg.version().startswith("multians_gb300")
+
+
+def test_plan_and_aux_sizes(mg):
+    p = mg.plan(50_000_000, 268_435_456, 1024)
+    assert p["block_units"] >= 4 and p["region_blocks"] >= 1 and p["walk_slots"] >= 1
+    need = mg.aux_size(50_000_000, p)
+    assert 0 < need <= mg.aux_size_max(50_000_000)
+    small = mg.plan(1000, 5000, 4096)
+    assert mg.aux_size(1000, small) <= mg.aux_size_max(1000)
+
+
+def test_table_check(mg, oracle_lib):
+    st = oracle_lib.make_stream(seed=1, lam=0.05, n=5000, L=1024)
+    assert mg.table_check(st.table) == 0
+    bad = st.table.copy()
+    bad[0] = bad[0] & 0x00ffffff | (20 << 24)
+    assert mg.table_check(bad) == -1
+    one = oracle_lib.encode(np.full(10, 9, dtype=np.uint8), 1024)
+    assert mg.table_check(one.table) == 1
+
+
+def test_decode_rejects_bad_arguments_without_gpu(mg):
+    """Argument checks run before any CUDA call."""
+    import ctypes
+    lib = mg.lib()
+    dummy = ctypes.c_void_p(16)
+    from multians_gb300._lib import Cfg
+    c = Cfg()
+    # first_state outside [L, 2L)
+    rc = lib.mans_decode(dummy, 10, dummy, 10, dummy, 1024, 5, 0, dummy, 1 << 20,
+                         ctypes.byref(c), None)
+    assert rc == mg.Status.ERR_ARG
+    # n_out == 0 is a no-op
+    assert lib.mans_decode(None, 0, None, 0, None, 1024, 1024, 0, None, 0, None, None) == 0
+    # aux too small
+    rc = lib.mans_decode(dummy, 1000, dummy, 1000, dummy, 1024, 1024, 0, dummy, 8,
+                         ctypes.byref(c), None)
+    assert rc == mg.Status.ERR_AUX_SMALL

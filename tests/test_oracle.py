@@ -1,0 +1,110 @@
+"""CPU tests: the C oracle pinned against the golden fixtures produced by the
+reference's own host code, and (where the reference sources are present)
+directly against that code."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+
+def sha(a) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _cases():
+    with open(os.path.join(GOLDEN, "golden.json")) as f:
+        return json.load(f)["cases"]
+
+
+@pytest.mark.parametrize("case", _cases(), ids=lambda c: f"s{c['seed']}_l{c['lambda']}_n{c['n']}_L{c['L']}")
+def test_oracle_matches_golden(oracle_lib, case):
+    O = oracle_lib
+    if case["n"] > (1 << 20):
+        pytest.skip("large case")
+    sym = O.gen_symbols(case["seed"], case["lambda"], case["n"])
+    assert sha(sym) == case["sha_symbols"]
+    st = O.encode(sym, case["L"])
+    assert st.n_units == case["n_units"]
+    assert st.first_bit == case["first_bit"]
+    assert st.first_state == case["first_state"]
+    assert sha(st.units) == case["sha_units"]
+    assert sha(st.table) == case["sha_table"]
+    dec = O.decode_seq(st)
+    assert sha(dec) == case["sha_decoded"]
+    assert np.array_equal(dec[::-1], sym)
+    if case["multicore_matches_source"] is not None:
+        mc, _ = O.multicore_decode(st, S=case["multicore_S"], T=case["multicore_T"])
+        # the port reproduces the reference multicore decoder, including its
+        # wrong output where a thread interval is shorter than the sync
+        # distance
+        assert sha(mc) == case["sha_multicore"]
+        assert np.array_equal(mc[::-1], sym) == case["multicore_matches_source"]
+
+
+@pytest.mark.parametrize("name", sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz")))
+def test_oracle_matches_array_fixture(oracle_lib, name):
+    O = oracle_lib
+    z = np.load(os.path.join(GOLDEN, name))
+    sym = z["symbols"]
+    L = int(z["table"].size)
+    st = O.encode(sym, L)
+    n_units, fb, fs = (int(v) for v in z["meta"])
+    assert (st.n_units, st.first_bit, st.first_state) == (n_units, fb, fs)
+    assert np.array_equal(st.units, z["units"])
+    assert np.array_equal(st.table, z["table"])
+    fx = O.Stream(sym, z["units"], n_units, fb, fs, z["table"], L)
+    assert np.array_equal(O.decode_seq(fx), z["decoded"])
+
+
+def test_sync_points_consistent(oracle_lib):
+    """Offsets of the true sync points reproduce the decoded output split."""
+    O = oracle_lib
+    st = O.make_stream(seed=11, lam=0.05, n=20_000, L=1024)
+    sp = O.sync_points(st, 4)
+    off = sp[:, 2].astype(np.int64)
+    assert off[0] == 0
+    assert np.all(np.diff(off) > 0)
+    assert off[-1] < st.n
+    assert np.all(sp[:, 3] >= st.L) and np.all(sp[:, 3] < 2 * st.L)
+    assert np.all(sp[:, 0] == 3)  # the last codeword sits in the last unit
+
+
+@pytest.mark.parametrize("T", [1, 2, 8])
+def test_multicore_port_roundtrip(oracle_lib, T):
+    O = oracle_lib
+    st = O.make_stream(seed=12, lam=0.2, n=200_000, L=1024)
+    mc, passes = O.multicore_decode(st, S=4, T=T)
+    assert passes >= 1
+    assert np.array_equal(mc[::-1], st.symbols)
+
+
+def test_single_symbol_multicore_reports(oracle_lib):
+    O = oracle_lib
+    st = O.encode(np.full(100, 3, dtype=np.uint8), 1024)
+    with pytest.raises(ValueError):
+        O.multicore_decode(st, S=4, T=1)
+    assert np.array_equal(O.decode_seq(st), np.full(100, 3, dtype=np.uint8))
+
+
+@pytest.mark.parametrize("lam", [0.005, 0.05, 0.2, 1.0, 2.0])
+@pytest.mark.parametrize("L", [1024, 4096])
+def test_oracle_vs_reference_build(oracle_lib, lam, L):
+    O = oracle_lib
+    if not O.ref_available():
+        pytest.skip("reference sources not built here")
+    for n in (5, 999, 70_001):
+        sym = O.gen_symbols(int(lam * 1e4) + n + L, lam, n)
+        a = O.encode(sym, L)
+        b = O.ref_encode(sym, L)
+        assert (a.n_units, a.first_bit, a.first_state) == (b.n_units, b.first_bit, b.first_state)
+        assert np.array_equal(a.units, b.units)
+        assert np.array_equal(a.table, b.table)
+        if n > 100:
+            ma, _ = O.multicore_decode(a, S=4, T=4)
+            mb = O.ref_multicore_decode(b, S=4, T=4)
+            assert np.array_equal(ma, mb)
