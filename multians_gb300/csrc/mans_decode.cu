@@ -47,9 +47,11 @@ namespace mans {
 struct DecodeParams {
     const uint32_t* units;
     uint8_t* out;
-    const uint32_t* table;
-    uint2* rec_g;          // [nblk]       Gamma_region records
-    uint2* rec_w;          // [nblk*dmax]  walk records, slot d-1 = Gamma_{r-d}
+    const uint32_t* table;      // reference-format table (L words)
+    uint2* tab_sync;            // [L] prepared counting table
+    uint2* tab_sym;             // [L] prepared symbol table
+    uint2* rec_g;               // [nblk]       Gamma_region records
+    uint2* rec_w;               // [nblk*dmax]  walk records, slot d-1 = Gamma_{r-d}
     unsigned long long* m;      // [nreg] merge bit position (~0 = none)
     long long* delta;           // [nreg]
     unsigned long long* Mpre;   // [nreg] prefix max of m
@@ -65,50 +67,108 @@ struct DecodeParams {
     uint32_t dmax;         // walk slots
     uint32_t nblk;
     uint32_t nreg;
+    uint32_t stage_cap;    // staging bytes per warp in k_final (multiple of 16)
 };
 
-// record: x = bit offset from the block start | state index << 8; y = count
-__device__ __forceinline__ uint2 make_rec(uint64_t pos, uint64_t bstart,
-                                          uint32_t idx, uint32_t cnt) {
-    return make_uint2((uint32_t) (pos - bstart) | (idx << 8), cnt);
+// Checks and converts the reference table, then builds both shared-memory
+// tables (see mans_device.cuh).  One CTA.  Invalid entries (outside
+// [L, 2L), or zero-bit entries that do not strictly decrease the state)
+// become safe one-bit entries and set MANS_DEV_BAD_TABLE; a table whose
+// every entry is a zero-bit self loop is a single-symbol table and sets
+// MANS_DEV_DEGENERATE.  Zero-bit runs are folded by pointer doubling over
+// the run-successor links (runs are strictly decreasing, so they end).
+__global__ void k_prep(DecodeParams p) {
+    extern __shared__ uint32_t sm[];
+    const uint32_t L = p.L;
+    uint32_t* plain = sm;                        // base | k << 16 | sym << 24
+    uint16_t* nxt0 = reinterpret_cast<uint16_t*>(sm + L);
+    uint16_t* nxt1 = nxt0 + L;
+    uint16_t* z0 = nxt1 + L;
+    uint16_t* z1 = z0 + L;
+    int bad_l = 0, loop_l = 1;
+    for (uint32_t j = threadIdx.x; j < L; j += blockDim.x) {
+        const uint32_t raw = __ldg(p.table + j);
+        const uint32_t ns = raw & 0xffffu, sym = (raw >> 16) & 0xffu, k = raw >> 24;
+        bool ok = false, sl = false;
+        uint32_t base = 0;
+        if (k <= kMaxBits) {
+            const uint64_t lo = (uint64_t) ns << k, hi = (uint64_t) (ns + 1) << k;
+            if (lo >= L && hi <= 2ull * L) {
+                base = (uint32_t) (lo - L);
+                ok = k > 0 || base < j;
+                sl = k == 0 && base == j;
+            }
+        }
+        uint32_t kk = k;
+        if (!ok) { base = 0; kk = 1; }
+        bad_l |= ok ? 0 : 1;
+        loop_l &= sl ? 1 : 0;
+        plain[j] = base | (kk << 16) | (sym << 24);
+        nxt0[j] = (uint16_t) (kk == 0 ? base : j);
+        z0[j] = (uint16_t) (kk == 0 ? 1 : 0);
+    }
+    const int any_bad = __syncthreads_or(bad_l);
+    const int all_loop = __syncthreads_and(loop_l);
+    if (threadIdx.x == 0 && any_bad)
+        atomicOr(p.status, all_loop ? MANS_DEV_DEGENERATE : MANS_DEV_BAD_TABLE);
+    // pointer doubling: nxt -> last state of the run, z -> run length
+    uint16_t *na = nxt0, *nb = nxt1, *za = z0, *zb = z1;
+    for (uint32_t span = 1; span < L; span <<= 1) {
+        for (uint32_t j = threadIdx.x; j < L; j += blockDim.x) {
+            const uint32_t t = na[j];
+            nb[j] = na[t];
+            const uint32_t zz = (uint32_t) za[j] + za[t];
+            zb[j] = (uint16_t) min(zz, 0xffffu);
+        }
+        __syncthreads();
+        uint16_t* tmp = na; na = nb; nb = tmp;
+        tmp = za; za = zb; zb = tmp;
+    }
+    for (uint32_t j = threadIdx.x; j < L; j += blockDim.x) {
+        const uint32_t e = plain[j];
+        const uint32_t k = (e >> 16) & 31u;
+        const uint32_t mask = (1u << k) - 1u;
+        p.tab_sym[j] = make_uint2((e & 0xffffu) * 8u, mask | (k << 16) | (e & 0xff000000u));
+        const uint32_t run = za[j];
+        if (run + 1 <= kIncMax) {
+            const uint32_t t = plain[na[j]];
+            const uint32_t kt = (t >> 16) & 31u;
+            p.tab_sync[j] = make_uint2((t & 0xffffu) * 8u,
+                                       ((1u << kt) - 1u) | (kt << 16) | ((run + 1) << 21));
+        } else {
+            p.tab_sync[j] = make_uint2((e & 0xffffu) * 8u, mask | (k << 16) | (1u << 21));
+        }
+    }
 }
 
-__global__ void k_sync(DecodeParams p) {
-    extern __shared__ uint32_t s_tbl[];
-    int any_bad, all_loop;
-    load_table(s_tbl, p.table, p.L, any_bad, all_loop);
-    if (any_bad) {
-        if (blockIdx.x == 0 && threadIdx.x == 0)
-            atomicOr(p.status, all_loop ? MANS_DEV_DEGENERATE : MANS_DEV_BAD_TABLE);
-        return;
-    }
+__device__ __forceinline__ uint2 make_rec(uint32_t rel, uint32_t idx, uint32_t cnt) {
+    return make_uint2(rel | (idx << 8), cnt);
+}
+
+__global__ void __launch_bounds__(128) k_sync(DecodeParams p) {
+    extern __shared__ __align__(16) uint2 s_tab[];
+    load_prepared(s_tab, p.tab_sync, p.L);
+    if (*(volatile uint32_t*) p.status & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE)) return;
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= p.nreg) return;
 
-    const uint64_t blk_bits = (uint64_t) p.B * 32;
+    const uint32_t tb = smem_addr(s_tab);
+    const uint32_t Bbits = p.B * 32;
     const uint32_t b0 = k * p.nb;
     const uint32_t b1 = min(b0 + p.nb, p.nblk);
-    const uint64_t end_bits = (uint64_t) p.nblk * blk_bits;
+    const uint64_t origin = (uint64_t) b0 * Bbits;
+    const uint32_t* __restrict__ in = p.units;
+    const uint32_t n = p.n_units;
 
     // Gamma_k inside region k
-    BitCursor a;
-    uint32_t ia;
-    if (k == 0) {
-        a.init(p.units, p.n_units, p.first_pos);
-        ia = p.first_idx;
-    } else {
-        a.init(p.units, p.n_units, (uint64_t) b0 * blk_bits);
-        ia = p.first_idx;
-    }
+    Cursor a;
+    a.init(in, n, origin, k == 0 ? (uint64_t) p.first_pos : origin, tb + 8u * p.first_idx);
     uint32_t ca = 0;
-    for (uint32_t b = b0; b < b1; ++b) {
-        const uint64_t bs = (uint64_t) b * blk_bits;
-        const uint64_t be = bs + blk_bits;
-        p.rec_g[b] = make_rec(a.pos, bs, ia, ca);
-        while (a.pos < be) {
-            a.step(s_tbl, ia);
-            ++ca;
-        }
+    uint32_t bs = 0;
+    for (uint32_t b = b0; b < b1; ++b, bs += Bbits) {
+        p.rec_g[b] = make_rec(a.pos - bs, entry_index(a.a, tb), ca);
+        const uint32_t be = bs + Bbits;
+        while (a.pos < be) ca += a.step(in, n) >> 21;
     }
     if (k + 1 >= p.nreg) {
         p.m[k] = ~0ull;
@@ -116,49 +176,36 @@ __global__ void k_sync(DecodeParams p) {
         return;
     }
 
-    // walk: Gamma_k (cursor a) against a replay of Gamma_{k+1} (cursor g)
-    BitCursor g;
-    uint32_t ig = p.first_idx;
-    g.init(p.units, p.n_units, (uint64_t) b1 * blk_bits);
+    // walk: Gamma_k (a) against a replay of Gamma_{k+1} (g), compared at
+    // every block start; both cursors step in the same loop iteration
+    Cursor g;
+    g.init(in, n, origin, (uint64_t) b1 * Bbits, tb + 8u * p.first_idx);
     uint32_t cg = 0;
-    uint32_t bn = b1;  // next block whose start cursor a has to record
-    for (;;) {
-        while (bn < p.nblk && a.pos >= (uint64_t) bn * blk_bits) {
-            const uint32_t d = bn / p.nb - k;
+    uint32_t d = 1, next_region = b1 + p.nb;
+    for (uint32_t bn = b1; bn < p.nblk; ++bn, bs += Bbits) {
+        if (bn == next_region) {
+            ++d;
+            next_region += p.nb;
             if (d > p.dmax) {
                 atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
                 p.m[k] = ~0ull;
                 p.delta[k] = 0;
                 return;
             }
-            p.rec_w[(size_t) bn * p.dmax + (d - 1)] =
-                make_rec(a.pos, (uint64_t) bn * blk_bits, ia, ca);
-            ++bn;
         }
-        if (a.pos >= end_bits && g.pos >= end_bits) {
-            // no merge before the stream end
-            p.m[k] = ~0ull;
-            p.delta[k] = 0;
+        while (a.pos < bs || g.pos < bs) {
+            if (a.pos < bs) ca += a.step(in, n) >> 21;
+            if (g.pos < bs) cg += g.step(in, n) >> 21;
+        }
+        p.rec_w[(size_t) bn * p.dmax + (d - 1)] = make_rec(a.pos - bs, entry_index(a.a, tb), ca);
+        if (a.pos == g.pos && a.a == g.a) {
+            p.m[k] = origin + a.pos;
+            p.delta[k] = (long long) ca - (long long) cg;
             return;
         }
-        if (a.pos == g.pos) {
-            if (ia == ig) {
-                p.m[k] = a.pos;
-                p.delta[k] = (long long) ca - (long long) cg;
-                return;
-            }
-            a.step(s_tbl, ia);
-            ++ca;
-            g.step(s_tbl, ig);
-            ++cg;
-        } else if (a.pos < g.pos) {
-            a.step(s_tbl, ia);
-            ++ca;
-        } else {
-            g.step(s_tbl, ig);
-            ++cg;
-        }
     }
+    p.m[k] = ~0ull;   // no merge before the stream end
+    p.delta[k] = 0;
 }
 
 // Exclusive prefix max of m (identity 0) and prefix sum of delta; one CTA.
@@ -202,55 +249,118 @@ __global__ void k_scan(DecodeParams p) {
     }
 }
 
-__global__ void k_final(DecodeParams p) {
-    extern __shared__ uint32_t s_tbl[];
-    int any_bad, all_loop;
-    load_table(s_tbl, p.table, p.L, any_bad, all_loop);
-    if (any_bad) {
-        if (all_loop) {
-            // single-symbol table: every state decodes that symbol
-            const uint8_t sym = (uint8_t) (__ldg(p.table) >> 16);
-            const unsigned long long stride = (unsigned long long) gridDim.x * blockDim.x;
-            for (unsigned long long i = (unsigned long long) blockIdx.x * blockDim.x + threadIdx.x;
-                 i < p.n_out; i += stride)
-                p.out[i] = sym;
-        }
-        return;
-    }
-    if (*(volatile uint32_t*) p.status & MANS_DEV_SYNC_OVERFLOW) return;
-    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= p.nblk) return;
-
-    const uint64_t blk_bits = (uint64_t) p.B * 32;
-    const uint64_t bs = (uint64_t) b * blk_bits;
-    const uint64_t be = bs + blk_bits;
+// Entry (bit offset from the block start, state index) and global output
+// offset of block b.  Returns false when no trajectory owns the block (a
+// walk ran out of slots).
+__device__ __forceinline__ bool block_entry(const DecodeParams& p, uint32_t b,
+                                            uint32_t& rel, uint32_t& idx,
+                                            unsigned long long& off) {
+    const uint64_t bs = (uint64_t) b * p.B * 32;
     const uint32_t r = b / p.nb;
     uint32_t d = 0;
     for (;; ++d) {
-        if (d > r || d > p.dmax) {
-            atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
-            return;
-        }
+        if (d > r || d > p.dmax) return false;
         if (p.Mpre[r - d] <= bs) break;
     }
-    const uint32_t k = r - d;
     const uint2 rec = d == 0 ? p.rec_g[b] : p.rec_w[(size_t) b * p.dmax + (d - 1)];
-    unsigned long long off = (unsigned long long) (p.Dpre[k] + (long long) rec.y);
-    uint32_t idx = rec.x >> 8;
-    BitCursor c;
-    c.init(p.units, p.n_units, bs + (rec.x & 0xffu));
-    while (c.pos < be) {
-        const uint32_t e = c.step(s_tbl, idx);
-        if (off < p.n_out) p.out[off] = (uint8_t) (e >> 24);
-        ++off;
+    off = (unsigned long long) (p.Dpre[r - d] + (long long) rec.y);
+    idx = rec.x >> 8;
+    rel = rec.x & 0xffu;
+    return true;
+}
+
+// One warp per 32 consecutive blocks.  The 32 blocks' symbols form one
+// contiguous output range; lanes decode their block into a shared staging
+// buffer laid out with the same 16-byte phase as the output, then the warp
+// writes the range with 16-byte stores (bytes at the unaligned ends).  A
+// range larger than the staging buffer is written byte by byte instead.
+__global__ void __launch_bounds__(128) k_final(DecodeParams p) {
+    extern __shared__ __align__(16) uint2 s_tab[];
+    load_prepared(s_tab, p.tab_sym, p.L);
+    const uint32_t st = *(volatile uint32_t*) p.status;
+    if (st & MANS_DEV_DEGENERATE) {
+        // single-symbol table: every state decodes that symbol
+        const uint8_t sym = (uint8_t) (__ldg(p.table) >> 16);
+        const unsigned long long stride = (unsigned long long) gridDim.x * blockDim.x;
+        for (unsigned long long i = (unsigned long long) blockIdx.x * blockDim.x + threadIdx.x;
+             i < p.n_out; i += stride)
+            p.out[i] = sym;
+        return;
     }
+    if (st & (MANS_DEV_BAD_TABLE | MANS_DEV_SYNC_OVERFLOW)) return;
+
+    const uint32_t tb = smem_addr(s_tab);
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint8_t* stage = reinterpret_cast<uint8_t*>(s_tab + p.L) + (size_t) warp * (p.stage_cap + 16);
+    const uint32_t b0 = blockIdx.x * blockDim.x + (warp << 5);
+    if (b0 >= p.nblk) return;
+    const uint32_t b = b0 + lane;
+    const bool have = b < p.nblk;
+
+    uint32_t rel = 0, idx = 0;
+    unsigned long long off = 0;
+    bool ok = have ? block_entry(p, b, rel, idx, off) : true;
+    unsigned long long off_end = p.n_out;   // offset one past this warp's blocks
+    if ((lane == 31 || b + 1 == p.nblk) && b + 1 < p.nblk) {
+        uint32_t tr, ti;
+        ok &= block_entry(p, b + 1, tr, ti, off_end);
+    }
+    if (__any_sync(0xffffffffu, !ok)) {
+        if (lane == 0) atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
+        return;
+    }
+    const unsigned long long off0 = __shfl_sync(0xffffffffu, off, 0);
+    const uint32_t last_lane = min(31u, p.nblk - 1 - b0);
+    off_end = __shfl_sync(0xffffffffu, off_end, last_lane);
+    const unsigned long long lo = min(off0, p.n_out);
+    const unsigned long long hi = min(max(off_end, off0), p.n_out);
+    const uint32_t phase = (uint32_t) (((uintptr_t) p.out + off0) & 15u);
+    const bool staged = hi - lo + phase <= p.stage_cap;
+
+    if (have) {
+        const uint32_t Bbits = p.B * 32;
+        const uint64_t bs = (uint64_t) b * Bbits;
+        const uint32_t* __restrict__ in = p.units;
+        const uint32_t n = p.n_units;
+        Cursor c;
+        c.init(in, n, bs, bs + rel, tb + 8u * idx);
+        if (staged) {
+            uint8_t* dst = stage + phase - off0;
+            while (c.pos < Bbits) {
+                const uint32_t y = c.step(in, n);
+                if (off < hi) dst[off] = (uint8_t) (y >> 24);
+                ++off;
+            }
+        } else {
+            while (c.pos < Bbits) {
+                const uint32_t y = c.step(in, n);
+                if (off < p.n_out) p.out[off] = (uint8_t) (y >> 24);
+                ++off;
+            }
+        }
+    }
+    if (!staged || lo >= hi) return;
+    __syncwarp();
+    // [lo, hi) from stage[phase + (i - off0)]; aligned middle in 16 B words
+    const uintptr_t base = (uintptr_t) p.out;
+    unsigned long long a0 = lo + ((16 - ((base + lo) & 15)) & 15);
+    unsigned long long a1 = hi - ((base + hi) & 15);
+    if (a0 > a1) a0 = a1 = hi;
+    for (unsigned long long i = lo + lane; i < a0; i += 32)
+        p.out[i] = stage[phase + (i - off0)];
+    for (unsigned long long i = a1 + lane; i < hi; i += 32)
+        p.out[i] = stage[phase + (i - off0)];
+    const uint4* src = reinterpret_cast<const uint4*>(stage + phase + (a0 - off0));
+    uint4* dst = reinterpret_cast<uint4*>(p.out + a0);
+    const uint32_t nvec = (uint32_t) ((a1 - a0) >> 4);
+    for (uint32_t v = lane; v < nvec; v += 32) dst[v] = src[v];
 }
 
 // ---------------------------------------------------------------------------
 // host side
 
 struct AuxLayout {
-    size_t rec_g, rec_w, m, delta, Mpre, Dpre, status, total;
+    size_t rec_g, rec_w, m, delta, Mpre, Dpre, status, tab_sync, tab_sym, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
@@ -259,6 +369,8 @@ static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax) {
     AuxLayout a;
     size_t o = 0;
     a.status = o; o += 256;
+    a.tab_sync = o; o += (size_t) kMaxStates * 8;
+    a.tab_sym = o; o += (size_t) kMaxStates * 8;
     a.rec_g = o; o += align256(nblk * sizeof(uint2));
     a.rec_w = o; o += align256(nblk * dmax * sizeof(uint2));
     a.m = o; o += align256(nreg * 8);
@@ -277,6 +389,14 @@ static uint32_t pow2_floor(uint64_t x) {
 
 static thread_local uint32_t g_last_launches = 0;
 
+// Blocks cover bit positions [0, 32 * n_units] inclusive: the first encoded
+// symbols can be zero-bit codewords sitting exactly at the stream end
+// (bit 32 * n_units), after the last bit the decoder consumes.  The
+// reference stops at the last unit and leaves them unwritten (its output
+// buffers are zero-filled, src/multicore_decoder.cc:176, and byte 0 is the
+// most frequent symbol of its generator, so its round trip passes).
+static size_t num_blocks(size_t n_units, size_t B) { return n_units / B + 1; }
+
 }  // namespace mans
 
 using namespace mans;
@@ -289,7 +409,7 @@ uint32_t mans_last_launch_count(void) { return g_last_launches; }
 
 int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
               mans_cfg* out) {
-    if (!out || n_units == 0 || L < 2 || L > 32768) return MANS_ERR_ARG;
+    if (!out || n_units == 0 || L < 2 || L > kMaxStates) return MANS_ERR_ARG;
     mans_cfg c = {0, 0, 0, 0};
     if (hint) c = *hint;
     const double sym_per_unit = n_out ? (double) n_out / (double) n_units : 1.0;
@@ -303,10 +423,13 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
         // keep at least ~4 regions per SM when the stream is small
         const uint64_t want_regions = 152ull * 4;
         while (R > 64 && n_units / R < want_regions) R /= 2;
-        c.region_blocks = (uint32_t) std::max<uint64_t>(1, R / c.block_units);
+        // an odd block count keeps lanes of a warp (one region each) off
+        // power-of-two strides, which would pile them into the same L1 sets
+        c.region_blocks = (uint32_t) std::max<uint64_t>(1, R / c.block_units) | 1u;
     }
     if (c.walk_slots == 0) c.walk_slots = 4;
     if (c.threads == 0) c.threads = 128;
+    c.threads = std::min<uint32_t>(128, std::max<uint32_t>(32, c.threads & ~31u));
     *out = c;
     return MANS_OK;
 }
@@ -314,7 +437,7 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
 size_t mans_aux_size(size_t n_units, const mans_cfg* cfg) {
     if (!cfg || cfg->block_units == 0 || cfg->region_blocks == 0 || cfg->walk_slots == 0)
         return 0;
-    const size_t nblk = (n_units + cfg->block_units - 1) / cfg->block_units;
+    const size_t nblk = num_blocks(n_units, cfg->block_units);
     const size_t nreg = (nblk + cfg->region_blocks - 1) / cfg->region_blocks;
     return layout_for(nblk, nreg, cfg->walk_slots).total;
 }
@@ -350,12 +473,12 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     if (n_out == 0) return MANS_OK;
     if (!d_units || !d_out || !d_table || !d_aux || n_units == 0 ||
         n_units > 0xffffffffull || L < 2 || L > 32768 || first_state < L ||
-        first_state >= 2 * L || first_bit > 32)
+        first_state >= 2 * L || first_bit > 32 || L > kMaxStates)
         return MANS_ERR_ARG;
     mans_cfg cfg;
     int rc = mans_plan(n_units, n_out, L, cfg_in, &cfg);
     if (rc != MANS_OK) return rc;
-    const size_t nblk = (n_units + cfg.block_units - 1) / cfg.block_units;
+    const size_t nblk = num_blocks(n_units, cfg.block_units);
     const size_t nreg = (nblk + cfg.region_blocks - 1) / cfg.region_blocks;
     const AuxLayout lay = layout_for(nblk, nreg, cfg.walk_slots);
     if (aux_bytes < lay.total) return MANS_ERR_AUX_SMALL;
@@ -374,6 +497,8 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     p.Mpre = (unsigned long long*) (base + lay.Mpre);
     p.Dpre = (long long*) (base + lay.Dpre);
     p.status = (uint32_t*) (base + lay.status);
+    p.tab_sync = (uint2*) (base + lay.tab_sync);
+    p.tab_sym = (uint2*) (base + lay.tab_sym);
     p.n_out = n_out;
     p.n_units = (uint32_t) n_units;
     p.L = L;
@@ -387,18 +512,26 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
 
     if (cudaMemsetAsync(p.status, 0, sizeof(uint32_t), st) != cudaSuccess)
         return MANS_ERR_CUDA;
-    const size_t smem = (size_t) L * sizeof(uint32_t);
+    const size_t smem = (size_t) L * sizeof(uint2);
     static bool attr_set = false;
     if (!attr_set) {
+        cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
         cudaFuncSetAttribute(k_sync, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-        cudaFuncSetAttribute(k_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+        cudaFuncSetAttribute(k_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
     const uint32_t T = cfg.threads;
+    // staging per warp: 1.5x the expected symbols of 32 blocks, 16 B rounded
+    const double per_unit = (double) n_out / (double) n_units;
+    uint64_t cap = (uint64_t) (per_unit * 32.0 * cfg.block_units * 1.5) + 256;
+    cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
+    p.stage_cap = (uint32_t) ((cap + 15) & ~(uint64_t) 15);
+    const size_t smem_final = smem + (size_t) (T / 32) * (p.stage_cap + 16);
+    k_prep<<<1, 1024, (size_t) L * 12, st>>>(p);
     k_sync<<<(unsigned) ((nreg + T - 1) / T), T, smem, st>>>(p);
     k_scan<<<1, 1024, 0, st>>>(p);
-    k_final<<<(unsigned) ((nblk + T - 1) / T), T, smem, st>>>(p);
-    g_last_launches = 3;
+    k_final<<<(unsigned) ((nblk + T - 1) / T), T, smem_final, st>>>(p);
+    g_last_launches = 4;
     if (cudaGetLastError() != cudaSuccess) return MANS_ERR_CUDA;
     return MANS_OK;
 }

@@ -1,5 +1,5 @@
 // Device building blocks of the GB300 MULTIANS decoder: the shared-memory
-// decode table and the per-thread bit cursor.
+// decode tables and the per-thread bit cursor.
 //
 // Decode step (the reference's per-symbol body, src/multians_gpu_decoder.cu
 // :131-167): with state x in [L, 2L) and table word t = table[x - L] =
@@ -7,108 +7,113 @@
 // and moves to x' = (next_state << k) | b; the symbol is emitted.  Every
 // table the reference generator builds keeps x' in [L, 2L), so the
 // reference's extra-bit loop (lines 141-145) never runs; the table check
-// below enforces that form and rejects anything else.
+// enforces that form and rejects anything else.
 //
-// Internal table word (one per state index j = x - L), 32 bits:
-//   bits  0..15  base  = (next_state << k) - L  (next index = base + b)
-//   bits 16..20  k     (bits consumed, 0..16)
-//   bits 24..31  symbol
+// Shared-memory entry (8 bytes per state index j = x - L):
+//   x  byte address (shared window) of the entry of state index
+//      base = (next_state << k) - L; the next entry is at x + 8 * b
+//   y  bits  0..15  mask = (1 << k) - 1
+//      bits 16..20  k
+//      bits 21..31  (counting table) codewords this step stands for
+//      bits 24..31  (symbol table)   the symbol
+// so one step is: e = lds64(a); b = buf & e.y & 0xffff; a = e.x + 8 * b --
+// two integer operations between dependent shared loads.
+//
+// The counting table folds runs of zero-bit codewords: from state j the
+// decoder may pass z zero-bit codewords (no bits read, state strictly
+// decreasing) before a codeword that reads bits.  Its entry for j is the
+// entry of that last codeword with a count of z + 1, so one step advances
+// to the next bit position.  Positions where a step starts are exactly the
+// first codewords at each bit position, which is all the sync logic needs.
 #pragma once
 
 #include <cstdint>
 
 namespace mans {
 
-constexpr uint32_t kMaxBits = 16;  // longest code a table word can carry
+constexpr uint32_t kMaxBits = 16;      // longest code a table word can carry
+constexpr uint32_t kMaxStates = 8192;  // L limit of the shared tables
+constexpr uint32_t kIncMax = 2047;     // longest folded run (11 bits)
 
-// Converts one reference table word into the internal form.  Entries that
-// would leave [L, 2L), or zero-bit entries that do not strictly decrease
-// the state index (a zero-bit cycle would never advance the stream), are
-// replaced by a safe one-bit entry and reported through `bad`.  `selfloop`
-// reports zero-bit entries that map a state to itself (all entries of a
-// single-symbol table look like that).
-__device__ __forceinline__ uint32_t convert_entry(uint32_t raw, uint32_t j,
-                                                  uint32_t L, bool& bad,
-                                                  bool& selfloop) {
-    const uint32_t ns = raw & 0xffffu;
-    const uint32_t sym = (raw >> 16) & 0xffu;
-    const uint32_t k = raw >> 24;
-    selfloop = false;
-    if (k <= kMaxBits) {
-        const uint64_t lo = (uint64_t) ns << k;
-        const uint64_t hi = (uint64_t) (ns + 1) << k;
-        if (lo >= L && hi <= 2ull * L) {
-            const uint32_t base = (uint32_t) (lo - L);
-            if (k > 0 || base < j) return base | (k << 16) | (sym << 24);
-            selfloop = (base == j);
-        }
-    }
-    bad = true;
-    return (1u << 16) | (sym << 24);
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return (uint32_t) __cvta_generic_to_shared(p);
 }
 
-// Loads and converts the table into shared memory (all threads of the CTA
-// take part).  Returns through the flags whether any entry was invalid and
-// whether every entry was a zero-bit self loop (single-symbol table).
-__device__ __forceinline__ void load_table(uint32_t* s_tbl,
-                                           const uint32_t* __restrict__ raw,
-                                           uint32_t L, int& any_bad,
-                                           int& all_selfloop) {
-    int bad_local = 0, loop_all = 1;
+__device__ __forceinline__ uint2 lds64(uint32_t a) {
+    uint2 v;
+    asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
+    return v;
+}
+
+// Copies a prepared table (global, x fields relative to the table start)
+// into shared memory, rebasing x to shared addresses.  All threads.
+__device__ __forceinline__ void load_prepared(uint2* s_tab, const uint2* __restrict__ g_tab,
+                                              uint32_t L) {
+    const uint32_t base = smem_addr(s_tab);
     for (uint32_t j = threadIdx.x; j < L; j += blockDim.x) {
-        bool bad = false, sl = false;
-        s_tbl[j] = convert_entry(__ldg(raw + j), j, L, bad, sl);
-        bad_local |= bad ? 1 : 0;
-        loop_all &= sl ? 1 : 0;
+        uint2 e = __ldg(g_tab + j);
+        e.x += base;
+        s_tab[j] = e;
     }
-    any_bad = __syncthreads_or(bad_local);
-    all_selfloop = __syncthreads_and(loop_all);
+    __syncthreads();
 }
 
-// Sequential reader of the stream bits, LSB first, starting at any bit
-// position.  Keeps 32..63 valid bits in a 64-bit buffer; units at index
-// >= n read as zero (the padding of the reference input buffer).
-struct BitCursor {
-    const uint32_t* __restrict__ in;
-    uint64_t buf;
-    uint64_t pos;      // global bit position of the next unread bit
-    uint32_t n;        // units in the stream
-    uint32_t next;     // next unit to load into buf
-    uint32_t nbits;    // valid bits in buf
+// Stream bit reader for one decoder, LSB first.  A 64-bit window lo:hi
+// holds 32..63 valid bits; the next unit is prefetched into `pre` one
+// refill ahead so the global load latency stays off the decode chain.
+// Positions are bit offsets relative to `origin` (a 64-bit bit address).
+// Units at index >= n read as zero.
+struct Cursor {
+    uint32_t a;      // shared address of the current state's entry
+    uint32_t lo, hi; // bit window
+    uint32_t avail;  // valid bits in the window
+    uint32_t pos;    // bit position of the next codeword (relative)
+    uint32_t next;   // global index of the unit in `pre`
+    uint32_t pre;    // prefetched unit
 
-    __device__ __forceinline__ uint32_t unit(uint32_t i) const {
+    __device__ __forceinline__ static uint32_t ld(const uint32_t* __restrict__ in,
+                                                  uint32_t n, uint32_t i) {
         return i < n ? __ldg(in + i) : 0u;
     }
 
-    __device__ __forceinline__ void init(const uint32_t* __restrict__ src,
-                                         uint32_t n_units, uint64_t p) {
-        in = src;
-        n = n_units;
-        pos = p;
-        const uint32_t u = (uint32_t) (p >> 5);
-        const uint32_t o = (uint32_t) (p & 31);
-        buf = ((uint64_t) unit(u) | ((uint64_t) unit(u + 1) << 32)) >> o;
-        nbits = 64 - o;
+    // Places the cursor at absolute bit position `abs` (pos = abs - origin).
+    __device__ __forceinline__ void init(const uint32_t* __restrict__ in, uint32_t n,
+                                         uint64_t origin, uint64_t abs,
+                                         uint32_t entry_addr) {
+        a = entry_addr;
+        pos = (uint32_t) (abs - origin);
+        const uint32_t u = (uint32_t) (abs >> 5), o = (uint32_t) (abs & 31);
+        const uint32_t w0 = ld(in, n, u), w1 = ld(in, n, u + 1);
+        lo = o ? __funnelshift_r(w0, w1, o) : w0;
+        hi = w1 >> o;
+        avail = 64 - o;
         next = u + 2;
+        pre = ld(in, n, next);
     }
 
-    // One decode step from state index `idx`; returns the table word used.
-    __device__ __forceinline__ uint32_t step(const uint32_t* s_tbl,
-                                             uint32_t& idx) {
-        const uint32_t e = s_tbl[idx];
-        const uint32_t k = (e >> 16) & 31u;
-        const uint32_t bits = (uint32_t) buf & ((1u << k) - 1u);
-        idx = (e & 0xffffu) + bits;
-        buf >>= k;
-        nbits -= k;
+    // One step; returns the entry's y word (mask / k / count or symbol).
+    __device__ __forceinline__ uint32_t step(const uint32_t* __restrict__ in, uint32_t n) {
+        const uint2 e = lds64(a);
+        const uint32_t b = lo & e.y & 0xffffu;
+        a = e.x + (b << 3);
+        const uint32_t k = (e.y >> 16) & 31u;
+        lo = __funnelshift_r(lo, hi, k);
+        hi >>= k;
+        avail -= k;
         pos += k;
-        if (nbits < 32) {
-            buf |= (uint64_t) unit(next) << nbits;
+        if (avail < 32) {
+            lo |= pre << avail;
+            hi = pre >> (32 - avail);
+            avail += 32;
             ++next;
-            nbits += 32;
+            pre = ld(in, n, next);
         }
-        return e;
+        return e.y;
     }
 };
+
+__device__ __forceinline__ uint32_t entry_index(uint32_t a, uint32_t tab_base) {
+    return (a - tab_base) >> 3;
+}
 
 }  // namespace mans
