@@ -43,6 +43,7 @@ typedef enum {
 #define MANS_DEV_SYNC_OVERFLOW  0x2u   /* a walk needed more slots */
 #define MANS_DEV_DEGENERATE     0x4u   /* single-symbol table: filled */
 #define MANS_DEV_COUNT_MISMATCH 0x8u   /* final pass disagreed with scan */
+#define MANS_DEV_SCAN_TIMEOUT   0x10u  /* a bounded device wait gave up */
 
 /* Launch geometry of one decode.  Zero fields are chosen by the built-in
  * autotuner from (L, units, output size). */

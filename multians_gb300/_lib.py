@@ -12,6 +12,7 @@ DEV_BAD_TABLE = 0x1
 DEV_SYNC_OVERFLOW = 0x2
 DEV_DEGENERATE = 0x4
 DEV_COUNT_MISMATCH = 0x8
+DEV_SCAN_TIMEOUT = 0x10
 
 
 class Status(enum.IntEnum):

@@ -208,44 +208,114 @@ __global__ void __launch_bounds__(128) k_sync(DecodeParams p) {
     p.delta[k] = 0;
 }
 
-// Exclusive prefix max of m (identity 0) and prefix sum of delta; one CTA.
-__global__ void k_scan(DecodeParams p) {
-    __shared__ unsigned long long s_max[1024];
-    __shared__ long long s_sum[1024];
-    const uint32_t T = blockDim.x, t = threadIdx.x;
-    const uint32_t n = p.nreg;
-    const uint32_t chunk = (n + T - 1) / T;
-    const uint32_t lo = min(t * chunk, n), hi = min(lo + chunk, n);
-    unsigned long long mx = 0;
-    long long sm = 0;
-    for (uint32_t i = lo; i < hi; ++i) {
-        mx = max(mx, p.m[i]);
-        sm += p.delta[i];
-    }
-    s_max[t] = mx;
-    s_sum[t] = sm;
+// Exclusive prefix max of m (identity 0) and prefix sum of delta over the
+// regions: single-pass decoupled look-back.  Tiles of kScanTile regions are
+// taken in launch order through an atomic ticket, so a tile only ever waits
+// on tiles that are already running or done; each wait is bounded and a
+// timeout sets MANS_DEV_SCAN_TIMEOUT instead of spinning on.
+constexpr uint32_t kScanThreads = 256;
+constexpr uint32_t kScanPer = 8;
+constexpr uint32_t kScanTile = kScanThreads * kScanPer;
+
+struct ScanTile {               // one per tile, 32 bytes
+    unsigned long long agg_m;   // tile max
+    long long agg_s;            // tile sum
+    unsigned long long inc_m;   // inclusive prefix max through this tile
+    long long inc_s;            // inclusive prefix sum
+};
+
+__global__ void __launch_bounds__(kScanThreads) k_scan(DecodeParams p, ScanTile* tiles,
+                                                      uint32_t* flags, uint32_t* ticket) {
+    __shared__ unsigned long long s_m[kScanThreads];
+    __shared__ long long s_s[kScanThreads];
+    __shared__ uint32_t s_tile;
+    __shared__ unsigned long long s_pm;
+    __shared__ long long s_ps;
+    const uint32_t t = threadIdx.x;
+    if (t == 0) s_tile = atomicAdd(ticket, 1u);
     __syncthreads();
-    for (uint32_t off = 1; off < T; off <<= 1) {
-        unsigned long long vm = 0;
-        long long vs = 0;
-        if (t >= off) {
-            vm = s_max[t - off];
-            vs = s_sum[t - off];
-        }
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * kScanTile + t * kScanPer;
+    unsigned long long vm[kScanPer];
+    long long vs[kScanPer];
+    unsigned long long lm = 0;
+    long long ls = 0;
+#pragma unroll
+    for (uint32_t i = 0; i < kScanPer; ++i) {
+        const uint32_t r = base + i;
+        vm[i] = r < p.nreg ? p.m[r] : 0ull;
+        vs[i] = r < p.nreg ? p.delta[r] : 0ll;
+        lm = max(lm, vm[i]);
+        ls += vs[i];
+    }
+    s_m[t] = lm;
+    s_s[t] = ls;
+    __syncthreads();
+    for (uint32_t off = 1; off < kScanThreads; off <<= 1) {
+        unsigned long long xm = 0;
+        long long xs = 0;
+        if (t >= off) { xm = s_m[t - off]; xs = s_s[t - off]; }
         __syncthreads();
-        if (t >= off) {
-            s_max[t] = max(s_max[t], vm);
-            s_sum[t] += vs;
-        }
+        if (t >= off) { s_m[t] = max(s_m[t], xm); s_s[t] += xs; }
         __syncthreads();
     }
-    unsigned long long run_m = t ? s_max[t - 1] : 0ull;
-    long long run_s = t ? s_sum[t - 1] : 0ll;
-    for (uint32_t i = lo; i < hi; ++i) {
-        p.Mpre[i] = run_m;
-        p.Dpre[i] = run_s;
-        run_m = max(run_m, p.m[i]);
-        run_s += p.delta[i];
+    if (t == kScanThreads - 1) {
+        const unsigned long long am = s_m[t];
+        const long long as = s_s[t];
+        unsigned long long pm = 0;
+        long long ps = 0;
+        if (tile == 0) {
+            tiles[0].inc_m = am;
+            tiles[0].inc_s = as;
+            __threadfence();
+            atomicExch(flags + 0, 2u);
+        } else {
+            tiles[tile].agg_m = am;
+            tiles[tile].agg_s = as;
+            __threadfence();
+            atomicExch(flags + tile, 1u);
+            // look back
+            int32_t j = (int32_t) tile - 1;
+            uint32_t spins = 0;
+            while (j >= 0) {
+                const uint32_t f = *(volatile uint32_t*) (flags + j);
+                if (f == 0) {
+                    if (++spins > (1u << 24)) {
+                        atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
+                        break;
+                    }
+                    continue;
+                }
+                __threadfence();
+                if (f == 2) {
+                    pm = max(pm, *(volatile unsigned long long*) &tiles[j].inc_m);
+                    ps += *(volatile long long*) &tiles[j].inc_s;
+                    break;
+                }
+                pm = max(pm, *(volatile unsigned long long*) &tiles[j].agg_m);
+                ps += *(volatile long long*) &tiles[j].agg_s;
+                --j;
+            }
+            tiles[tile].inc_m = max(pm, am);
+            tiles[tile].inc_s = ps + as;
+            __threadfence();
+            atomicExch(flags + tile, 2u);
+        }
+        s_pm = pm;
+        s_ps = ps;
+    }
+    __syncthreads();
+    unsigned long long run_m = max(s_pm, t ? s_m[t - 1] : 0ull);
+    long long run_s = s_ps + (t ? s_s[t - 1] : 0ll);
+#pragma unroll
+    for (uint32_t i = 0; i < kScanPer; ++i) {
+        const uint32_t r = base + i;
+        if (r < p.nreg) {
+            p.Mpre[r] = run_m;
+            p.Dpre[r] = run_s;
+        }
+        run_m = max(run_m, vm[i]);
+        run_s += vs[i];
     }
 }
 
@@ -287,7 +357,7 @@ __global__ void __launch_bounds__(128) k_final(DecodeParams p) {
             p.out[i] = sym;
         return;
     }
-    if (st & (MANS_DEV_BAD_TABLE | MANS_DEV_SYNC_OVERFLOW)) return;
+    if (st & (MANS_DEV_BAD_TABLE | MANS_DEV_SYNC_OVERFLOW | MANS_DEV_SCAN_TIMEOUT)) return;
 
     const uint32_t tb = smem_addr(s_tab);
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -360,7 +430,8 @@ __global__ void __launch_bounds__(128) k_final(DecodeParams p) {
 // host side
 
 struct AuxLayout {
-    size_t rec_g, rec_w, m, delta, Mpre, Dpre, status, tab_sync, tab_sym, total;
+    size_t rec_g, rec_w, m, delta, Mpre, Dpre, status, tab_sync, tab_sym, scan_tiles,
+        scan_flags, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
@@ -377,6 +448,9 @@ static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax) {
     a.delta = o; o += align256(nreg * 8);
     a.Mpre = o; o += align256(nreg * 8);
     a.Dpre = o; o += align256(nreg * 8);
+    const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
+    a.scan_tiles = o; o += align256(ntiles * sizeof(ScanTile));
+    a.scan_flags = o; o += align256((ntiles + 1) * 4);   // flags, then the ticket
     a.total = o;
     return a;
 }
@@ -510,7 +584,9 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     p.nblk = (uint32_t) nblk;
     p.nreg = (uint32_t) nreg;
 
-    if (cudaMemsetAsync(p.status, 0, sizeof(uint32_t), st) != cudaSuccess)
+    const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
+    if (cudaMemsetAsync(p.status, 0, sizeof(uint32_t), st) != cudaSuccess ||
+        cudaMemsetAsync(base + lay.scan_flags, 0, (ntiles + 1) * 4, st) != cudaSuccess)
         return MANS_ERR_CUDA;
     const size_t smem = (size_t) L * sizeof(uint2);
     static bool attr_set = false;
@@ -529,7 +605,9 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     const size_t smem_final = smem + (size_t) (T / 32) * (p.stage_cap + 16);
     k_prep<<<1, 1024, (size_t) L * 12, st>>>(p);
     k_sync<<<(unsigned) ((nreg + T - 1) / T), T, smem, st>>>(p);
-    k_scan<<<1, 1024, 0, st>>>(p);
+    k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(
+        p, (ScanTile*) (base + lay.scan_tiles), (uint32_t*) (base + lay.scan_flags),
+        (uint32_t*) (base + lay.scan_flags) + ntiles);
     k_final<<<(unsigned) ((nblk + T - 1) / T), T, smem_final, st>>>(p);
     g_last_launches = 4;
     if (cudaGetLastError() != cudaSuccess) return MANS_ERR_CUDA;
@@ -578,6 +656,7 @@ int mans_decode_sync(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     if (status_out) *status_out = st;
     if (st & MANS_DEV_BAD_TABLE) return MANS_ERR_TABLE;
     if (st & MANS_DEV_SYNC_OVERFLOW) return MANS_ERR_SYNC;
+    if (st & MANS_DEV_SCAN_TIMEOUT) return MANS_ERR_CUDA;
     return MANS_OK;
 }
 

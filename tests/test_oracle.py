@@ -37,13 +37,16 @@ def test_oracle_matches_golden(oracle_lib, case):
     dec = O.decode_seq(st)
     assert sha(dec) == case["sha_decoded"]
     assert np.array_equal(dec[::-1], sym)
-    if case["multicore_matches_source"] is not None:
+    if case["multicore_matches_source"]:
+        # Where every thread interval is longer than the sync distance the
+        # multicore method is exact and the port reproduces the reference.
+        # Elsewhere the reference races (a thread reads its predecessor's
+        # last sync point while the predecessor may still rewrite it,
+        # multicore_decoder.cc:57-75, 136-143) and both outputs depend on
+        # thread timing, so they are not compared.
         mc, _ = O.multicore_decode(st, S=case["multicore_S"], T=case["multicore_T"])
-        # the port reproduces the reference multicore decoder, including its
-        # wrong output where a thread interval is shorter than the sync
-        # distance
         assert sha(mc) == case["sha_multicore"]
-        assert np.array_equal(mc[::-1], sym) == case["multicore_matches_source"]
+        assert np.array_equal(mc[::-1], sym)
 
 
 @pytest.mark.parametrize("name", sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz")))
@@ -104,7 +107,10 @@ def test_oracle_vs_reference_build(oracle_lib, lam, L):
         assert (a.n_units, a.first_bit, a.first_state) == (b.n_units, b.first_bit, b.first_state)
         assert np.array_equal(a.units, b.units)
         assert np.array_equal(a.table, b.table)
-        if n > 100:
+        if n > 50_000:
+            # thread intervals (>= 2000 units) exceed the sync distance here,
+            # where the reference method is exact and race-free
             ma, _ = O.multicore_decode(a, S=4, T=4)
             mb = O.ref_multicore_decode(b, S=4, T=4)
             assert np.array_equal(ma, mb)
+            assert np.array_equal(ma[::-1], sym)
