@@ -40,6 +40,7 @@
 #include <cstring>
 
 #include "mans_device.cuh"
+#include "mans_tma.cuh"
 #include "multians_gb300.h"
 
 namespace mans {
@@ -134,9 +135,9 @@ __global__ void k_prep(DecodeParams p) {
             const uint32_t t = plain[na[j]];
             const uint32_t kt = (t >> 16) & 31u;
             p.tab_sync[j] = make_uint2((t & 0xffffu) * 8u,
-                                       ((1u << kt) - 1u) | (kt << 16) | ((run + 1) << 21));
+                                       ((1u << kt) - 1u) | (kt << 16) | ((run + 1) << 24));
         } else {
-            p.tab_sync[j] = make_uint2((e & 0xffffu) * 8u, mask | (k << 16) | (1u << 21));
+            p.tab_sync[j] = make_uint2((e & 0xffffu) * 8u, mask | (k << 16) | (1u << 24));
         }
     }
 }
@@ -145,67 +146,183 @@ __device__ __forceinline__ uint2 make_rec(uint32_t rel, uint32_t idx, uint32_t c
     return make_uint2(rel | (idx << 8), cnt);
 }
 
-__global__ void __launch_bounds__(128) k_sync(DecodeParams p) {
+// k_sync staging: every lane owns a ring of kRingSlots chunks of kChunk
+// units in shared memory, filled by TMA bulk copies.  The warp works in
+// rounds; in one round every lane advances its cursor(s) to the next block
+// start (at most kMaxBlockUnits units plus a step).  Between rounds each
+// lane releases its oldest chunk w once its cursors have loaded past unit
+// 32(w+1) + kRelease (a cursor re-started at a block start may re-read up
+// to 3 units behind the other's load point) and refills that slot with
+// chunk w + 4.  Reads stay inside chunks w and w + 1 (the two walk cursors
+// start a round at most one step apart, so a round reads below
+// 32(w+1) + kRelease + 3 + kMaxBlockUnits + 2 < 32(w+2)), so a chunk
+// copied in round r is first read in round r + 2 and round r waits only
+// for the copies of round r - 2.
+constexpr uint32_t kChunk = 32;                    // units per ring slot
+constexpr uint32_t kRingSlots = 4;
+constexpr uint32_t kRingUnits = kChunk * kRingSlots;
+constexpr uint32_t kRingStride = kRingUnits * 4 + 16;   // bytes per lane (padded)
+constexpr uint32_t kRelease = 4;
+constexpr uint32_t kSyncThreads = 64;
+constexpr uint32_t kMaxBlockUnits = 16;
+
+enum : uint32_t { kModeG = 0, kModeWalk = 1, kModeDone = 2 };
+
+__device__ __forceinline__ void ring_fill(uint32_t slot_addr, const uint32_t* __restrict__ in,
+                                          uint32_t n, uint32_t chunk, uint32_t bar,
+                                          uint32_t& bytes) {
+    const uint32_t u = chunk * kChunk;
+    if (u + kChunk <= n) {
+        tma_load(slot_addr, in + u, kChunk * 4, bar);
+        bytes = kChunk * 4;
+    } else {
+        for (uint32_t i = 0; i < kChunk; ++i)
+            sts32(slot_addr + i * 4, u + i < n ? __ldg(in + u + i) : 0u);
+        bytes = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kSyncThreads) k_sync(DecodeParams p) {
     extern __shared__ __align__(16) uint2 s_tab[];
     load_prepared(s_tab, p.tab_sync, p.L);
     if (*(volatile uint32_t*) p.status & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE)) return;
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= p.nreg) return;
-
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t tb = smem_addr(s_tab);
-    const uint32_t Bbits = p.B * 32;
-    const uint32_t b0 = k * p.nb;
-    const uint32_t b1 = min(b0 + p.nb, p.nblk);
-    const uint64_t origin = (uint64_t) b0 * Bbits;
+    const uint32_t tab_bytes = (p.L * 8 + 15) & ~15u;
+    const uint32_t ring = tb + tab_bytes + threadIdx.x * kRingStride;
+    const uint32_t bars = tb + tab_bytes + blockDim.x * kRingStride + warp * 40;  // 5 mbarriers
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t* __restrict__ in = p.units;
     const uint32_t n = p.n_units;
+    const uint32_t Bbits = p.B * 32;
+    const UnitSrc rs{ring, 0u, kRingUnits - 1, kRingUnits - 1};
 
-    // Gamma_k inside region k
-    Cursor a;
-    a.init(in, n, origin, k == 0 ? (uint64_t) p.first_pos : origin, tb + 8u * p.first_idx);
-    uint32_t ca = 0;
-    uint32_t bs = 0;
-    for (uint32_t b = b0; b < b1; ++b, bs += Bbits) {
-        p.rec_g[b] = make_rec(a.pos - bs, entry_index(a.a, tb), ca);
-        const uint32_t be = bs + Bbits;
-        while (a.pos < be) ca += a.step(in, n) >> 21;
+    if ((blockIdx.x * blockDim.x + (warp << 5)) >= p.nreg) return;   // whole warp idle
+    if (lane == 0) {
+        for (uint32_t i = 0; i < 5; ++i) mbar_init(bars + 8 * i, 1);
+        fence_mbar_init();
     }
-    if (k + 1 >= p.nreg) {
-        p.m[k] = ~0ull;
-        p.delta[k] = 0;
-        return;
-    }
+    __syncwarp();
 
-    // walk: Gamma_k (a) against a replay of Gamma_{k+1} (g), compared at
-    // every block start; both cursors step in the same loop iteration
-    Cursor g;
-    g.init(in, n, origin, (uint64_t) b1 * Bbits, tb + 8u * p.first_idx);
-    uint32_t cg = 0;
-    uint32_t d = 1, next_region = b1 + p.nb;
-    for (uint32_t bn = b1; bn < p.nblk; ++bn, bs += Bbits) {
-        if (bn == next_region) {
-            ++d;
-            next_region += p.nb;
-            if (d > p.dmax) {
-                atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
-                p.m[k] = ~0ull;
-                p.delta[k] = 0;
-                return;
+    uint32_t mode = k < p.nreg ? kModeG : kModeDone;
+    const uint32_t b0 = min(k * p.nb, p.nblk);
+    const uint32_t b1 = min(b0 + p.nb, p.nblk);
+    const uint64_t origin = (uint64_t) b0 * Bbits;
+    const uint64_t start = k == 0 ? (uint64_t) p.first_pos : origin;
+    uint32_t w = (uint32_t) (start >> 5) / kChunk;   // oldest chunk held
+    bool timed_out = false;
+
+    // initial fill: chunks w .. w+3, completion on barrier 4
+    {
+        uint32_t mine = 0;
+        if (mode != kModeDone) {
+            fence_proxy_async();
+            for (uint32_t i = 0; i < kRingSlots; ++i) {
+                uint32_t by;
+                ring_fill(ring + ((w + i) & (kRingSlots - 1)) * kChunk * 4, in, n, w + i,
+                          bars + 32, by);
+                mine += by;
             }
         }
-        while (a.pos < bs || g.pos < bs) {
-            if (a.pos < bs) ca += a.step(in, n) >> 21;
-            if (g.pos < bs) cg += g.step(in, n) >> 21;
+        const uint32_t total = __reduce_add_sync(0xffffffffu, mine);
+        if (lane == 0) mbar_arrive_expect_tx(bars + 32, total);
+        if (!mbar_wait(bars + 32, 0)) {
+            timed_out = true;
+            mbar_wait(bars + 32, 0);
         }
-        p.rec_w[(size_t) bn * p.dmax + (d - 1)] = make_rec(a.pos - bs, entry_index(a.a, tb), ca);
-        if (a.pos == g.pos && a.a == g.a) {
-            p.m[k] = origin + a.pos;
-            p.delta[k] = (long long) ca - (long long) cg;
-            return;
+        __syncwarp();
+    }
+
+    SCursor A, G;
+    uint32_t ca = 0, cg = 0;
+    uint32_t b = b0;        // G: block being decoded; walk: block start to reach
+    uint32_t bs = 0;        // relative start bit of block b
+    uint32_t d = 1, next_region = 0;
+    if (mode == kModeG) {
+        A.init(rs, origin, start, tb + 8u * p.first_idx);
+        p.rec_g[b0] = make_rec(A.pos, entry_index(A.a, tb), 0);
+        if (b0 == b1) mode = kModeDone;
+    }
+
+    uint32_t r = 0;
+    while (__any_sync(0xffffffffu, mode != kModeDone)) {
+        // refill: wait for round r-2's copies, then issue this round's
+        if (r >= 2 && !mbar_wait(bars + 8 * ((r - 2) & 3), ((r - 2) >> 2) & 1)) {
+            timed_out = true;
+            mbar_wait(bars + 8 * ((r - 2) & 3), ((r - 2) >> 2) & 1);
+        }
+        uint32_t mine = 0;
+        if (mode != kModeDone) {
+            const uint32_t lowest = mode == kModeWalk ? min(A.next, G.next) : A.next;
+            if (lowest >= (w + 1) * kChunk + kRelease) {
+                fence_proxy_async();
+                ring_fill(ring + (w & (kRingSlots - 1)) * kChunk * 4, in, n, w + kRingSlots,
+                          bars + 8 * (r & 3), mine);
+                ++w;
+            }
+        }
+        const uint32_t total = __reduce_add_sync(0xffffffffu, mine);
+        if (lane == 0) mbar_arrive_expect_tx(bars + 8 * (r & 3), total);
+        ++r;
+
+        if (mode == kModeG) {
+            // decode to the end of block b, record block b+1's entry
+            const uint32_t be = bs + Bbits;
+            while (A.pos < be) ca += A.step(rs) >> 24;
+            ++b;
+            bs = be;
+            if (b < b1) {
+                p.rec_g[b] = make_rec(A.pos - bs, entry_index(A.a, tb), ca);
+            } else if (k + 1 >= p.nreg) {
+                p.m[k] = ~0ull;
+                p.delta[k] = 0;
+                mode = kModeDone;
+            } else {
+                // walk Gamma_k (A) against a replay of Gamma_{k+1} (G)
+                G.init(rs, origin, (uint64_t) b1 * Bbits, tb + 8u * p.first_idx);
+                next_region = b1 + p.nb;
+                mode = kModeWalk;
+            }
+        }
+        if (mode == kModeWalk) {
+            // both cursors are at (or past) the start of block b
+            while (A.pos < bs || G.pos < bs) {
+                if (A.pos < bs) ca += A.step(rs) >> 24;
+                if (G.pos < bs) cg += G.step(rs) >> 24;
+            }
+            p.rec_w[(size_t) b * p.dmax + (d - 1)] = make_rec(A.pos - bs, entry_index(A.a, tb), ca);
+            if (A.pos == G.pos && A.a == G.a) {
+                p.m[k] = origin + A.pos;
+                p.delta[k] = (long long) ca - (long long) cg;
+                mode = kModeDone;
+            } else {
+                ++b;
+                bs += Bbits;
+                if (b >= p.nblk) {
+                    p.m[k] = ~0ull;   // no merge before the stream end
+                    p.delta[k] = 0;
+                    mode = kModeDone;
+                } else if (b == next_region) {
+                    ++d;
+                    next_region += p.nb;
+                    if (d > p.dmax) {
+                        atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
+                        p.m[k] = ~0ull;
+                        p.delta[k] = 0;
+                        mode = kModeDone;
+                    }
+                }
+            }
         }
     }
-    p.m[k] = ~0ull;   // no merge before the stream end
-    p.delta[k] = 0;
+    // drain: no copy may still be writing this CTA's shared memory at exit
+    for (uint32_t q = (r >= 2 ? r - 2 : 0); q < r; ++q) {
+        if (!mbar_wait(bars + 8 * (q & 3), (q >> 2) & 1)) {
+            timed_out = true;
+            mbar_wait(bars + 8 * (q & 3), (q >> 2) & 1);
+        }
+    }
+    if (timed_out) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
 }
 
 // Exclusive prefix max of m (identity 0) and prefix sum of delta over the
@@ -334,17 +451,29 @@ __device__ __forceinline__ bool block_entry(const DecodeParams& p, uint32_t b,
     }
     const uint2 rec = d == 0 ? p.rec_g[b] : p.rec_w[(size_t) b * p.dmax + (d - 1)];
     off = (unsigned long long) (p.Dpre[r - d] + (long long) rec.y);
-    idx = rec.x >> 8;
-    rel = rec.x & 0xffu;
+    idx = min(rec.x >> 8, p.L - 1);   // records come from k_sync; the clamp keeps
+    rel = rec.x & 0xffu;              // table addresses in range regardless
     return true;
 }
 
-// One warp per 32 consecutive blocks.  The 32 blocks' symbols form one
-// contiguous output range; lanes decode their block into a shared staging
-// buffer laid out with the same 16-byte phase as the output, then the warp
-// writes the range with 16-byte stores (bytes at the unaligned ends).  A
-// range larger than the staging buffer is written byte by byte instead.
-__global__ void __launch_bounds__(128) k_final(DecodeParams p) {
+// One warp per 32 consecutive blocks, one lane per block.  Each lane's
+// input (its block plus four units of look-ahead) arrives in shared memory
+// by a TMA bulk copy into a lane-private tile; the tiles sit kTileStride
+// bytes apart so lanes reading the same relative unit spread over eight
+// bank groups.  The symbol count of every block is known from the scan, so
+// a lane decodes exactly that many symbols (and checks that it ended at
+// the next block start).  The 32 blocks' symbols form one contiguous output
+// range; lanes decode into a shared staging buffer laid out with the same
+// 16-byte phase as the output, then the warp writes the range with 16-byte
+// stores (bytes at the unaligned ends).  A range larger than the staging
+// buffer is written byte by byte instead.
+constexpr uint32_t kFinalThreads = 128;
+
+__device__ __forceinline__ void sts8(uint32_t a, uint32_t v) {
+    asm volatile("st.shared.u8 [%0], %1;" :: "r"(a), "r"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(kFinalThreads) k_final(DecodeParams p) {
     extern __shared__ __align__(16) uint2 s_tab[];
     load_prepared(s_tab, p.tab_sym, p.L);
     const uint32_t st = *(volatile uint32_t*) p.status;
@@ -361,57 +490,105 @@ __global__ void __launch_bounds__(128) k_final(DecodeParams p) {
 
     const uint32_t tb = smem_addr(s_tab);
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint8_t* stage = reinterpret_cast<uint8_t*>(s_tab + p.L) + (size_t) warp * (p.stage_cap + 16);
+    const uint32_t tile_units = p.B + 4;                 // 16-byte multiple (B % 4 == 0)
+    const uint32_t tile_stride = tile_units * 4 + (((tile_units * 4) & 127) == 0 ? 16 : 0);
+    const uint32_t per_warp = 32 * tile_stride + 16 + p.stage_cap + 16;
+    const uint32_t tab_bytes = (p.L * 8 + 15) & ~15u;
+    const uint32_t wbase = tb + tab_bytes + warp * per_warp;
+    const uint32_t tile = wbase + lane * tile_stride;
+    const uint32_t bar = wbase + 32 * tile_stride;       // 16 bytes reserved
+    const uint32_t stage_addr = bar + 16;
+
     const uint32_t b0 = blockIdx.x * blockDim.x + (warp << 5);
     if (b0 >= p.nblk) return;
     const uint32_t b = b0 + lane;
     const bool have = b < p.nblk;
 
+    // stage the lane tiles
+    const uint32_t* __restrict__ in = p.units;
+    const uint32_t n = p.n_units;
+    const uint32_t u0 = b * p.B;
+    if (lane == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    const uint32_t avail_units = (have && u0 < n) ? min(tile_units, n - u0) : 0u;
+    const uint32_t bulk_units = avail_units & ~3u;
+    const uint32_t total = __reduce_add_sync(0xffffffffu, bulk_units * 4);
+    if (lane == 0) mbar_arrive_expect_tx(bar, total);
+    __syncwarp();
+    if (bulk_units) {
+        fence_proxy_async();
+        tma_load(tile, in + u0, bulk_units * 4, bar);
+    }
+    for (uint32_t i = bulk_units; i < tile_units; ++i)
+        sts32(tile + i * 4, i < avail_units ? __ldg(in + u0 + i) : 0u);
+
     uint32_t rel = 0, idx = 0;
     unsigned long long off = 0;
     bool ok = have ? block_entry(p, b, rel, idx, off) : true;
-    unsigned long long off_end = p.n_out;   // offset one past this warp's blocks
-    if ((lane == 31 || b + 1 == p.nblk) && b + 1 < p.nblk) {
+    unsigned long long off_nx = p.n_out;   // offset of block b + 1
+    const unsigned long long from_next = __shfl_down_sync(0xffffffffu, off, 1);
+    if (lane < 31 && b + 1 < p.nblk) off_nx = from_next;
+    if (lane == 31 && b + 1 < p.nblk) {
         uint32_t tr, ti;
-        ok &= block_entry(p, b + 1, tr, ti, off_end);
+        ok &= block_entry(p, b + 1, tr, ti, off_nx);
     }
-    if (__any_sync(0xffffffffu, !ok)) {
-        if (lane == 0) atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
+    bool staged_in = mbar_wait(bar, 0);
+    if (!staged_in) mbar_wait(bar, 0);   // never exit with the copy in flight
+    __syncwarp();
+    if (__any_sync(0xffffffffu, !ok || !staged_in)) {
+        if (lane == 0) atomicOr(p.status, staged_in ? MANS_DEV_SYNC_OVERFLOW : MANS_DEV_SCAN_TIMEOUT);
         return;
     }
     const unsigned long long off0 = __shfl_sync(0xffffffffu, off, 0);
     const uint32_t last_lane = min(31u, p.nblk - 1 - b0);
-    off_end = __shfl_sync(0xffffffffu, off_end, last_lane);
+    const unsigned long long off_end = __shfl_sync(0xffffffffu, off_nx, last_lane);
     const unsigned long long lo = min(off0, p.n_out);
     const unsigned long long hi = min(max(off_end, off0), p.n_out);
     const uint32_t phase = (uint32_t) (((uintptr_t) p.out + off0) & 15u);
     const bool staged = hi - lo + phase <= p.stage_cap;
 
+    // every lane's range must lie inside the warp's range (offsets are
+    // monotonic in the block index); anything else is reported, not written
+    const bool lane_ok = !have || (off >= off0 && max(off_nx, off) <= max(off_end, off0));
+    if (__any_sync(0xffffffffu, !lane_ok)) {
+        if (lane == 0) atomicOr(p.status, MANS_DEV_COUNT_MISMATCH);
+        return;
+    }
     if (have) {
-        const uint32_t Bbits = p.B * 32;
-        const uint64_t bs = (uint64_t) b * Bbits;
-        const uint32_t* __restrict__ in = p.units;
-        const uint32_t n = p.n_units;
-        Cursor c;
-        c.init(in, n, bs, bs + rel, tb + 8u * idx);
+        // symbols of this block that land in [.., n_out)
+        const unsigned long long end = min(max(off_nx, off), p.n_out);
+        // a valid block holds at most (B * 32 + 17) bit positions, each with
+        // fewer than L codewords: the cap keeps a corrupted offset from
+        // running the loop (or its tile reads) away
+        const unsigned long long cap_sym = (unsigned long long) (p.B * 32 + 17) * p.L;
+        const uint32_t cnt = off < end ? (uint32_t) min(end - off, cap_sym) : 0u;
+        const uint32_t pos_cap = p.B * 32 + kMaxBits + 1;
+        const uint32_t full = off_nx >= off ? (uint32_t) min(off_nx - off, 0xffffffffull) : 0u;
+        SCursor c;
+        const UnitSrc ts{tile, u0, ~0u, tile_units - 1};
+        const uint64_t bs = (uint64_t) b * p.B * 32;   // cursor units are global indices
+        c.init(ts, bs, bs + rel, tb + 8u * idx);
         if (staged) {
-            uint8_t* dst = stage + phase - off0;
-            while (c.pos < Bbits) {
-                const uint32_t y = c.step(in, n);
-                if (off < hi) dst[off] = (uint8_t) (y >> 24);
-                ++off;
-            }
+            const uint32_t dst = stage_addr + phase + (uint32_t) (off - off0);
+            for (uint32_t i = 0; i < cnt && c.pos < pos_cap; ++i)
+                sts8(dst + i, c.step(ts) >> 24);
         } else {
-            while (c.pos < Bbits) {
-                const uint32_t y = c.step(in, n);
-                if (off < p.n_out) p.out[off] = (uint8_t) (y >> 24);
-                ++off;
-            }
+            uint8_t* dst = p.out + off;
+            for (uint32_t i = 0; i < cnt && c.pos < pos_cap; ++i)
+                dst[i] = (uint8_t) (c.step(ts) >> 24);
         }
+        // a block decoded to its full count ends at the next block start
+        if (cnt == full && b + 1 < p.nblk &&
+            (c.pos < p.B * 32 || c.pos >= p.B * 32 + kMaxBits + 1))
+            atomicOr(p.status, MANS_DEV_COUNT_MISMATCH);
     }
     if (!staged || lo >= hi) return;
     __syncwarp();
     // [lo, hi) from stage[phase + (i - off0)]; aligned middle in 16 B words
+    const uint8_t* stage = reinterpret_cast<const uint8_t*>(s_tab) + (stage_addr - tb);
     const uintptr_t base = (uintptr_t) p.out;
     unsigned long long a0 = lo + ((16 - ((base + lo) & 15)) & 15);
     unsigned long long a1 = hi - ((base + hi) & 15);
@@ -492,6 +669,7 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
         uint64_t b = (uint64_t) (128.0 / std::max(sym_per_unit, 1e-3));
         c.block_units = std::min<uint32_t>(std::max<uint32_t>(pow2_floor(std::max<uint64_t>(b, 1)), 4), 256);
     }
+    c.block_units = std::min<uint32_t>(std::max<uint32_t>(c.block_units & ~3u, 4), kMaxBlockUnits);
     if (c.region_blocks == 0) {
         uint64_t R = L <= 1024 ? 512 : 2048;  // units per sync region
         // keep at least ~4 regions per SM when the stream is small
@@ -545,6 +723,7 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
                 size_t aux_bytes, const mans_cfg* cfg_in, void* stream) {
     g_last_launches = 0;
     if (n_out == 0) return MANS_OK;
+    if (((uintptr_t) d_units & 15) != 0) return MANS_ERR_ARG;   // TMA needs 16-byte alignment
     if (!d_units || !d_out || !d_table || !d_aux || n_units == 0 ||
         n_units > 0xffffffffull || L < 2 || L > 32768 || first_state < L ||
         first_state >= 2 * L || first_bit > 32 || L > kMaxStates)
@@ -588,7 +767,7 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     if (cudaMemsetAsync(p.status, 0, sizeof(uint32_t), st) != cudaSuccess ||
         cudaMemsetAsync(base + lay.scan_flags, 0, (ntiles + 1) * 4, st) != cudaSuccess)
         return MANS_ERR_CUDA;
-    const size_t smem = (size_t) L * sizeof(uint2);
+    const size_t smem = ((size_t) L * sizeof(uint2) + 15) & ~(size_t) 15;
     static bool attr_set = false;
     if (!attr_set) {
         cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
@@ -596,19 +775,22 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
         cudaFuncSetAttribute(k_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
-    const uint32_t T = cfg.threads;
     // staging per warp: 1.5x the expected symbols of 32 blocks, 16 B rounded
     const double per_unit = (double) n_out / (double) n_units;
     uint64_t cap = (uint64_t) (per_unit * 32.0 * cfg.block_units * 1.5) + 256;
     cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
     p.stage_cap = (uint32_t) ((cap + 15) & ~(uint64_t) 15);
-    const size_t smem_final = smem + (size_t) (T / 32) * (p.stage_cap + 16);
+    const size_t smem_sync = smem + (size_t) kSyncThreads * kRingStride + (kSyncThreads / 32) * 40;
+    const uint32_t tile_bytes = (cfg.block_units + 4) * 4;
+    const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
+    const size_t per_warp_final = (size_t) 32 * tile_stride + 16 + p.stage_cap + 16;
+    const size_t smem_final = smem + (size_t) (kFinalThreads / 32) * per_warp_final;
     k_prep<<<1, 1024, (size_t) L * 12, st>>>(p);
-    k_sync<<<(unsigned) ((nreg + T - 1) / T), T, smem, st>>>(p);
+    k_sync<<<(unsigned) ((nreg + kSyncThreads - 1) / kSyncThreads), kSyncThreads, smem_sync, st>>>(p);
     k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(
         p, (ScanTile*) (base + lay.scan_tiles), (uint32_t*) (base + lay.scan_flags),
         (uint32_t*) (base + lay.scan_flags) + ntiles);
-    k_final<<<(unsigned) ((nblk + T - 1) / T), T, smem_final, st>>>(p);
+    k_final<<<(unsigned) ((nblk + kFinalThreads - 1) / kFinalThreads), kFinalThreads, smem_final, st>>>(p);
     g_last_launches = 4;
     if (cudaGetLastError() != cudaSuccess) return MANS_ERR_CUDA;
     return MANS_OK;

@@ -13,9 +13,9 @@
 //   x  byte address (shared window) of the entry of state index
 //      base = (next_state << k) - L; the next entry is at x + 8 * b
 //   y  bits  0..15  mask = (1 << k) - 1
-//      bits 16..20  k
-//      bits 21..31  (counting table) codewords this step stands for
-//      bits 24..31  (symbol table)   the symbol
+//      bits 16..23  k
+//      bits 24..31  (counting table) codewords this step stands for
+//                   (symbol table)   the symbol
 // so one step is: e = lds64(a); b = buf & e.y & 0xffff; a = e.x + 8 * b --
 // two integer operations between dependent shared loads.
 //
@@ -33,7 +33,7 @@ namespace mans {
 
 constexpr uint32_t kMaxBits = 16;      // longest code a table word can carry
 constexpr uint32_t kMaxStates = 8192;  // L limit of the shared tables
-constexpr uint32_t kIncMax = 2047;     // longest folded run (11 bits)
+constexpr uint32_t kIncMax = 255;      // longest folded run (8 bits)
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
     return (uint32_t) __cvta_generic_to_shared(p);
@@ -99,7 +99,7 @@ struct Cursor {
         const uint2 e = lds64(a);
         const uint32_t b = lo & e.y & 0xffffu;
         a = e.x + (b << 3);
-        const uint32_t k = (e.y >> 16) & 31u;
+        const uint32_t k = __byte_perm(e.y, 0, 0x4442);
         lo = __funnelshift_r(lo, hi, k);
         hi >>= k;
         avail -= k;

@@ -1,0 +1,128 @@
+// TMA bulk copies (cp.async.bulk) and mbarriers for staging compressed
+// units into shared memory, plus the shared-memory bit cursor.
+//
+// Why shared memory: a decoder refills its 64-bit window every few symbols,
+// at a different step on every lane.  A refill from global memory leaves a
+// load in flight on the warp's register; the next step some other lane
+// refills and the warp waits for that load, so global latency lands on
+// nearly every step.  Shared-memory refills cost a shared load that
+// overlaps the table lookup of the next step.
+#pragma once
+
+#include <cstdint>
+
+#include "mans_device.cuh"
+
+namespace mans {
+
+__device__ __forceinline__ uint32_t lds32(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
+    return v;
+}
+
+__device__ __forceinline__ void sts32(uint32_t a, uint32_t v) {
+    asm volatile("st.shared.u32 [%0], %1;" :: "r"(a), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 :: "r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+// Waits for the phase with the given parity; gives up after a bounded
+// number of polls (returns false) instead of spinning forever.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < (1u << 22); ++i)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+
+// 1-D bulk copy global -> shared, completion counted on `bar` (bytes).
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void tma_load(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        :: "r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+
+// Where a cursor finds its units: the unit with global index i lives at
+// `base + min((i - u0) & wrap, last) * 4`.  A per-lane ring of 128 units
+// uses u0 = 0, wrap = last = 127; a flat tile uses wrap = ~0 and
+// last = tile length - 1.  The clamp keeps every shared address inside the
+// caller's buffer whatever the stream contents.
+struct UnitSrc {
+    uint32_t base, u0, wrap, last;
+    __device__ __forceinline__ uint32_t operator()(uint32_t i) const {
+        return lds32(base + (min((i - u0) & wrap, last) << 2));
+    }
+};
+
+// Bit cursor over units held in shared memory.  The window lo:hi holds the
+// bits [pos, top); a refill is due when fewer than 32 remain, i.e. when
+// pos > lim = top - 32.  Tracking top instead of a bit count saves an
+// update per step.
+struct SCursor {
+    uint32_t a;      // shared address of the current state's entry
+    uint32_t lo, hi; // bit window
+    uint32_t pos;    // bit position of the next codeword (relative)
+    uint32_t lim;    // refill when pos > lim
+    uint32_t next;   // global index of the next unit to load
+
+    __device__ __forceinline__ void init(const UnitSrc& src, uint64_t origin, uint64_t abs,
+                                         uint32_t entry_addr) {
+        a = entry_addr;
+        pos = (uint32_t) (abs - origin);
+        const uint32_t u = (uint32_t) (abs >> 5), o = (uint32_t) (abs & 31);
+        const uint32_t w0 = src(u), w1 = src(u + 1);
+        lo = __funnelshift_r(w0, w1, o);
+        hi = w1 >> o;
+        lim = pos - o + 32;     // top = pos - o + 64
+        next = u + 2;
+    }
+
+    // One step; returns y (mask | k << 16 | count-or-symbol << 24).
+    __device__ __forceinline__ uint32_t step(const UnitSrc& src) {
+        const uint2 e = lds64(a);
+        const uint32_t b = lo & e.y & 0xffffu;
+        a = e.x + (b << 3);
+        const uint32_t k = __byte_perm(e.y, 0, 0x4442);
+        lo = __funnelshift_r(lo, hi, k);
+        hi >>= k;
+        pos += k;
+        if (pos > lim) {
+            const uint32_t avail = lim + 32 - pos;   // 16..31
+            const uint32_t u = src(next);
+            lo |= u << avail;
+            hi = u >> (32 - avail);
+            lim += 32;
+            ++next;
+        }
+        return e.y;
+    }
+};
+
+}  // namespace mans
