@@ -1,0 +1,385 @@
+"""Benchmark of the MULTIANS decode path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload plain|batched|served] [--mb 256] [--lam 0.05] [--L 1024]
+
+One JSON line on stdout (rank 0).  The default workload is the plain
+single-stream decode of a 256 MB stream (lambda = 0.05, L = 1024 states):
+seeded synthetic uint8 symbols, the reference's table generator and encoder
+(the library's C++ implementation of them), one raw stream.
+
+  value   decoded GB/s (decoded bytes / s) with the stream and the output
+          resident in HBM; each step is one full decode (four kernels).
+  e2e     the same metric through the public C ABI with host buffers: per
+          step the pinned-host units and table go host->device, the decode
+          runs, the decoded bytes come back device->host.
+  roofline  the dominant kernel: algorithmic bytes per launch / its mean
+          launch time (CUDA events around every kernel in the timed
+          region), against the measured HBM copy bandwidth.
+  cpu_baseline  the reference's multicore CPU method on the host cores, on
+          a bounded sample of the same workload.
+
+Multi-GPU: the decode of one stream does not shard across processes here;
+every rank decodes its own replica stream ("replicas only", weak scaling)
+and value sums the ranks' decoded bytes over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "decoded GB/s on 1 GB300 (plain vs batched/served) + %HBM roofline; p50/p99; bit-exact"
+HBM_FALLBACK_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["plain", "batched", "served"], default="plain")
+    ap.add_argument("--mb", type=float, default=256.0, help="stream size in MiB of symbols")
+    ap.add_argument("--lam", type=float, default=0.05)
+    ap.add_argument("--L", type=int, default=1024)
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-mb", type=float, default=32.0)
+    return ap.parse_args()
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="mans_clocks_", suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=self.out, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.out.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for ln in f:
+                parts = [x.strip() for x in ln.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_workload(args, rank):
+    from multians_gb300 import host
+    n = int(args.mb * (1 << 20))
+    t0 = time.time()
+    st = host.make_stream(args.seed + rank, args.lam, n, args.L)
+    return st, time.time() - t0
+
+
+def cpu_baseline(st, sample_mb: float):
+    """The reference's multicore method (oracle port; the reference build
+    when present) on a bounded prefix-sized sample of the same workload."""
+    from oracle import oracle as O
+    n = min(st.n, int(sample_mb * (1 << 20)))
+    sym = st.symbols[:n]
+    sst = O.encode(sym, st.L)
+    cores = os.cpu_count() or 1
+    nsub = (sst.n_units + 3) // 4
+    T = max(1, min(cores, nsub))
+    use_ref = O.ref_available()
+    times = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        if use_ref:
+            out = O.ref_multicore_decode(sst, S=4, T=T)
+        else:
+            out, _ = O.multicore_decode(sst, S=4, T=T)
+        times.append(time.perf_counter() - t0)
+    ok = bool((out[::-1] == sym).all())
+    t = statistics.median(times)
+    return {"value": round(n / t / 1e9, 4), "unit": "GB/s", "cores": T,
+            "kind": "reference" if use_ref else "port",
+            "sample": f"{n >> 20} MiB prefix of the workload's symbols, re-encoded; "
+                      f"MulticoreDecoder method S=4, T={T}; median of 3; bit-exact={ok}"}
+
+
+def run_reference(args, ws, rank):
+    """The reference's own CPU implementation of the path on this workload
+    (oracle/_ref when built, else the oracle's restatement of it)."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    n = int(args.mb * (1 << 20))
+    st = O.make_stream(args.seed, args.lam, n, args.L)   # same bytes as the GPU arm's stream
+    ost = st
+    cores = os.cpu_count() or 1
+    T = max(1, min(cores, (st.n_units + 3) // 4))
+    use_ref = O.ref_available()
+    dec = (lambda: O.ref_multicore_decode(ost, S=4, T=T)) if use_ref else \
+        (lambda: O.multicore_decode(ost, S=4, T=T)[0])
+    for _ in range(max(0, min(args.warmup, 2))):
+        dec()
+    times = []
+    out = None
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out = dec()
+        times.append(time.perf_counter() - t0)
+    ok = bool((out[::-1] == st.symbols).all())
+    tot = sum(times)
+    v = st.n * len(times) / tot / 1e9
+    times_ms = sorted(x * 1e3 for x in times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GB/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(tot / len(times) * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": f"plain {args.mb:g}MiB lambda={args.lam} L={args.L}",
+                   "n_symbols": st.n, "n_units": st.n_units, "lambda": args.lam, "L": args.L,
+                   "seed": args.seed},
+        "bit_exact": ok,
+        "latency_ms": {"p50": round(times_ms[len(times_ms) // 2], 3),
+                       "p99": round(times_ms[min(len(times_ms) - 1, int(0.99 * len(times_ms)))], 3)},
+        "cpu_baseline": {"value": round(v, 4), "unit": "GB/s", "cores": T,
+                         "kind": "reference" if use_ref else "port",
+                         "sample": f"the full workload per step; MulticoreDecoder method S=4, T={T}"},
+        "e2e": {"value": round(v, 4), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+
+    import multians_gb300 as mg
+    from multians_gb300 import _lib
+    from multians_gb300.decoder import decode_async, aux_status
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    st, gen_s = make_workload(args, rank)
+    n = st.n
+    units_h = torch.from_numpy(st.units.view(np.int32)).pin_memory()
+    table_h = torch.from_numpy(st.table.view(np.int32)).pin_memory()
+    units = units_h.to(dev)
+    table = table_h.to(dev)
+    out = torch.empty(n, dtype=torch.uint8, device=dev)
+    out_h = torch.empty(n, dtype=torch.uint8).pin_memory()
+    cfg = mg.plan(st.n_units, n, st.L)
+    aux = torch.empty(mg.aux_size(st.n_units, cfg), dtype=torch.uint8, device=dev)
+    want = torch.from_numpy(np.ascontiguousarray(st.symbols[::-1])).to(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def one():
+        decode_async(units, st.n_units, out, n, table, st.L, st.first_state, st.first_bit,
+                     aux, cfg, stream=stream)
+
+    # warm-up + correctness
+    for _ in range(max(3, args.warmup)):
+        one()
+    status = aux_status(aux, stream)
+    bit_exact = bool(torch.equal(out, want)) and status == 0
+    del want
+
+    # timed region: device-resident decode
+    launches_per = mg.lib().mans_last_launch_count()
+    _lib.timing_enable(args.steps)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        evs[0].record(stream)
+        for i in range(args.steps):
+            one()
+            evs[i + 1].record(stream)
+        torch.cuda.synchronize(dev)
+    if ws > 1:
+        dist.barrier()
+    per_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
+    total_ms = evs[0].elapsed_time(evs[-1])
+    kern_ms, kern_n = _lib.timing_collect()
+    _lib.timing_enable(0)
+    status |= aux_status(aux, stream)
+    bit_exact = bit_exact and bool(torch.equal(out, torch.from_numpy(
+        np.ascontiguousarray(st.symbols[::-1])).to(dev))) and status == 0
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+
+    # e2e: host buffers through the C ABI, copies inside the timed region
+    h2d = st.units.nbytes + st.table.nbytes
+    d2h = n
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        units.copy_(units_h, non_blocking=True)
+        table.copy_(table_h, non_blocking=True)
+        one()
+        out_h.copy_(out, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        units.copy_(units_h, non_blocking=True)
+        table.copy_(table_h, non_blocking=True)
+        one()
+        out_h.copy_(out, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_ok = bool(np.array_equal(out_h.numpy(), st.symbols[::-1]))
+
+    if rank != 0:
+        if ws > 1:
+            dist.destroy_process_group()
+        return
+
+    ms = total_ms / args.steps
+    value = ws * n / (ms / 1e3) / 1e9
+    hbm, peak_kind = measured_peaks()
+    comp_bytes = st.n_units * 4
+    # dominant kernel and its algorithmic bytes per launch
+    mean_k = {k: v / max(1, kern_n) for k, v in kern_ms.items()}
+    dom = max(mean_k, key=lambda k: mean_k[k])
+    alg = {"k_sync": comp_bytes, "k_final": comp_bytes + n,
+           "k_prep": st.L * 4, "k_scan": 0}[dom]
+    achieved = alg / (mean_k[dom] / 1e3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    wl = f"plain {args.mb:g}MiB lambda={args.lam} L={args.L}"
+    if os.path.exists(tf):
+        with open(tf) as f:
+            for ln in f:
+                parts = ln.strip().split("\t")
+                if len(parts) == 3 and parts[0] == dom and parts[1] == wl:
+                    traffic = int(parts[2])
+    per_sorted = sorted(per_ms)
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_baseline(st, args.cpu_sample_mb)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic",
+        "config": {"workload": wl, "n_symbols": n, "n_units": st.n_units,
+                   "compressed_bytes": comp_bytes, "bits_per_symbol": round(st.bits_per_symbol, 4),
+                   "lambda": args.lam, "L": args.L, "seed": args.seed, "geometry": cfg,
+                   "l2": "inputs larger than L2 (stream + output > 129 MB), no flush",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "bit_exact": bit_exact,
+        "latency_ms": {"p50": round(per_sorted[len(per_sorted) // 2], 4),
+                       "p99": round(per_sorted[min(len(per_sorted) - 1,
+                                                   int(0.99 * len(per_sorted)))], 4)},
+        "decode_roofline": {"bytes": comp_bytes + n,
+                            "achieved_gbs": round((comp_bytes + n) / (ms / 1e3) / 1e9, 2),
+                            "frac_of_measured": round((comp_bytes + n) / (ms / 1e3) / 1e9 / hbm, 4),
+                            "frac_of_8tbs": round((comp_bytes + n) / (ms / 1e3) / 1e9 / 8000, 4)},
+        "kernel_ms": {k: round(v, 4) for k, v in mean_k.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2),
+                     "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": traffic,
+                     "alg_bytes_per_launch": alg},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(ws * n / (e2e_ms / 1e3) / 1e9, 3), "unit": "GB/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "bit_exact": e2e_ok},
+        "gpu_launches": launches_per * args.steps,
+        "clocks": clk.summary(),
+        "gen_seconds": round(gen_s, 2),
+    }
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    if args.workload != "plain":
+        from multians_gb300 import bench_workloads
+        bench_workloads.run(args, ws, rank, local)
+        return
+    run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

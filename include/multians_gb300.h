@@ -99,8 +99,35 @@ int mans_decode_sync(const uint32_t* d_units, size_t n_units,
  * single symbol (all entries are zero-bit self loops), -1 otherwise. */
 int mans_table_check(const uint32_t* h_table, uint32_t L);
 
+/* Per-kernel timing of decodes (no counterpart in the reference, which
+ * times whole decodes with cudaEvents in src/multians_util.cc:20-63).
+ * mans_timing_enable(n) makes the next n decodes record CUDA events around
+ * each of their kernels on the decode stream (n = 0 turns it off);
+ * mans_timing_collect waits for them and returns the summed milliseconds
+ * per kernel (prep, sync, scan, final) and how many decodes were timed. */
+int mans_timing_enable(int max_decodes);
+int mans_timing_collect(float* ms_per_kernel, int n_kernels, int* n_decodes);
+
 /* Number of kernels launched by the last decode on this thread. */
 uint32_t mans_last_launch_count(void);
+
+/* Host-side data preparation (the reference's ANSTableGenerator +
+ * ANSEncoder path, src/ans_table_generator.cc, src/ans_encoder.cc, as C
+ * calls).  mans_host_gen_symbols: n seeded symbols
+ * min(255, floor(-ln(U) / lambda)), U = ((x >> 11) + 1) * 2^-53, x from
+ * mt19937_64(seed).  mans_host_max_units: the unit capacity (padding
+ * included) mans_host_encode needs for these symbols.  mans_host_encode:
+ * builds the L-state table from the symbol counts
+ * (generate_distribution_from_buffer with `table_seed`, generate_table,
+ * generate_encoder_table, get_decoder_table) and encodes; writes the L
+ * decoder words, the units in CUHDInputBuffer order plus 4 zero units, the
+ * unit count and the first bit / first state.  sym must be readable one
+ * byte past n (the encoder looks one symbol ahead). */
+int mans_host_gen_symbols(uint64_t seed, double lambda, uint8_t* out, size_t n);
+size_t mans_host_max_units(const uint8_t* sym, size_t n, uint32_t L, uint32_t table_seed);
+int mans_host_encode(const uint8_t* sym, size_t n, uint32_t L, uint32_t table_seed,
+                     uint32_t* dec_table, uint32_t* units, size_t cap, size_t* n_units,
+                     uint32_t* first_bit, uint32_t* first_state);
 
 /* Library version string. */
 const char* mans_version(void);

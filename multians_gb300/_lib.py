@@ -61,6 +61,9 @@ SIGNATURES = {
     "mans_decode": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _u32, _u32, _u32, _vp, _sz,
                                    ctypes.POINTER(Cfg), _vp]),
     "mans_aux_status": (ctypes.c_int, [_vp, _vp, _u32p]),
+    "mans_timing_enable": (ctypes.c_int, [ctypes.c_int]),
+    "mans_timing_collect": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float), ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_int)]),
     "mans_decode_sync": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _u32, _u32, _u32, _vp, _sz,
                                         ctypes.POINTER(Cfg), _vp, _u32p]),
 }
@@ -117,3 +120,19 @@ def table_check(table) -> int:
     import numpy as np
     t = np.ascontiguousarray(table, dtype=np.uint32)
     return int(lib().mans_table_check(t.ctypes.data_as(_u32p), t.size))
+
+
+KERNELS = ("k_prep", "k_sync", "k_scan", "k_final")
+
+
+def timing_enable(max_decodes: int) -> None:
+    check(lib().mans_timing_enable(int(max_decodes)), "mans_timing_enable")
+
+
+def timing_collect() -> tuple[dict, int]:
+    """Summed milliseconds per kernel over the decodes timed since
+    timing_enable, and the number of decodes."""
+    buf = (ctypes.c_float * 4)()
+    n = ctypes.c_int(0)
+    check(lib().mans_timing_collect(buf, 4, ctypes.byref(n)), "mans_timing_collect")
+    return {k: float(buf[i]) for i, k in enumerate(KERNELS)}, int(n.value)

@@ -640,6 +640,21 @@ static uint32_t pow2_floor(uint64_t x) {
 
 static thread_local uint32_t g_last_launches = 0;
 
+// Optional per-kernel timing: events recorded around each kernel of every
+// decode into a ring of slots, summed by mans_timing_collect.
+constexpr int kTimedKernels = 4;   // prep, sync, scan, final
+struct TimingState {
+    bool on = false;
+    int cap = 0, used = 0;
+    cudaEvent_t* ev = nullptr;     // cap * (kTimedKernels + 1)
+};
+static TimingState g_timing;
+
+static void timing_mark(int slot_evt, cudaStream_t st) {
+    if (!g_timing.on || g_timing.used >= g_timing.cap) return;
+    cudaEventRecord(g_timing.ev[g_timing.used * (kTimedKernels + 1) + slot_evt], st);
+}
+
 // Blocks cover bit positions [0, 32 * n_units] inclusive: the first encoded
 // symbols can be zero-bit codewords sitting exactly at the stream end
 // (bit 32 * n_units), after the last bit the decoder consumes.  The
@@ -785,14 +800,53 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
     const size_t per_warp_final = (size_t) 32 * tile_stride + 16 + p.stage_cap + 16;
     const size_t smem_final = smem + (size_t) (kFinalThreads / 32) * per_warp_final;
+    timing_mark(0, st);
     k_prep<<<1, 1024, (size_t) L * 12, st>>>(p);
+    timing_mark(1, st);
     k_sync<<<(unsigned) ((nreg + kSyncThreads - 1) / kSyncThreads), kSyncThreads, smem_sync, st>>>(p);
+    timing_mark(2, st);
     k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(
         p, (ScanTile*) (base + lay.scan_tiles), (uint32_t*) (base + lay.scan_flags),
         (uint32_t*) (base + lay.scan_flags) + ntiles);
+    timing_mark(3, st);
     k_final<<<(unsigned) ((nblk + kFinalThreads - 1) / kFinalThreads), kFinalThreads, smem_final, st>>>(p);
+    timing_mark(4, st);
+    if (g_timing.on && g_timing.used < g_timing.cap) ++g_timing.used;
     g_last_launches = 4;
     if (cudaGetLastError() != cudaSuccess) return MANS_ERR_CUDA;
+    return MANS_OK;
+}
+
+int mans_timing_enable(int max_decodes) {
+    if (g_timing.ev) {
+        for (int i = 0; i < g_timing.cap * (kTimedKernels + 1); ++i) cudaEventDestroy(g_timing.ev[i]);
+        delete[] g_timing.ev;
+        g_timing.ev = nullptr;
+    }
+    g_timing.on = max_decodes > 0;
+    g_timing.cap = max_decodes > 0 ? max_decodes : 0;
+    g_timing.used = 0;
+    if (!g_timing.on) return MANS_OK;
+    g_timing.ev = new cudaEvent_t[(size_t) g_timing.cap * (kTimedKernels + 1)];
+    for (int i = 0; i < g_timing.cap * (kTimedKernels + 1); ++i)
+        if (cudaEventCreate(&g_timing.ev[i]) != cudaSuccess) return MANS_ERR_CUDA;
+    return MANS_OK;
+}
+
+int mans_timing_collect(float* ms_per_kernel, int n_kernels, int* n_decodes) {
+    if (!ms_per_kernel || n_kernels < kTimedKernels) return MANS_ERR_ARG;
+    for (int k = 0; k < n_kernels; ++k) ms_per_kernel[k] = 0.f;
+    for (int d = 0; d < g_timing.used; ++d) {
+        cudaEvent_t* e = g_timing.ev + d * (kTimedKernels + 1);
+        if (cudaEventSynchronize(e[kTimedKernels]) != cudaSuccess) return MANS_ERR_CUDA;
+        for (int k = 0; k < kTimedKernels; ++k) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, e[k], e[k + 1]) != cudaSuccess) return MANS_ERR_CUDA;
+            ms_per_kernel[k] += ms;
+        }
+    }
+    if (n_decodes) *n_decodes = g_timing.used;
+    g_timing.used = 0;
     return MANS_OK;
 }
 

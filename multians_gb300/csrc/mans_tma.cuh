@@ -81,12 +81,19 @@ struct UnitSrc {
     }
 };
 
-// Bit cursor over units held in shared memory.  The window lo:hi holds the
-// bits [pos, top); a refill is due when fewer than 32 remain, i.e. when
-// pos > lim = top - 32.  Tracking top instead of a bit count saves an
-// update per step.
+// Bit cursor over units held in shared memory, software-pipelined: the
+// table entry of the current state is already in registers (e), and each
+// step issues the shared load of the next entry before anything that
+// branches on this step's result, so the dependent chain per symbol is one
+// shared load plus two integer operations.  The window lo:hi holds the
+// bits [pos, top); a refill is due when fewer than 32 remain
+// (pos > lim = top - 32).  Every step loads the unit a refill would take,
+// together with the table entry and before either is needed: a load issued
+// only on the lanes that refill would leave the warp waiting on another
+// lane's load into the same register on most steps.
 struct SCursor {
-    uint32_t a;      // shared address of the current state's entry
+    uint2 e;         // table entry of the current state
+    uint32_t a;      // shared address of that entry
     uint32_t lo, hi; // bit window
     uint32_t pos;    // bit position of the next codeword (relative)
     uint32_t lim;    // refill when pos > lim
@@ -95,6 +102,7 @@ struct SCursor {
     __device__ __forceinline__ void init(const UnitSrc& src, uint64_t origin, uint64_t abs,
                                          uint32_t entry_addr) {
         a = entry_addr;
+        e = lds64(a);
         pos = (uint32_t) (abs - origin);
         const uint32_t u = (uint32_t) (abs >> 5), o = (uint32_t) (abs & 31);
         const uint32_t w0 = src(u), w1 = src(u + 1);
@@ -106,22 +114,23 @@ struct SCursor {
 
     // One step; returns y (mask | k << 16 | count-or-symbol << 24).
     __device__ __forceinline__ uint32_t step(const UnitSrc& src) {
-        const uint2 e = lds64(a);
-        const uint32_t b = lo & e.y & 0xffffu;
+        const uint32_t u = src(next);
+        const uint32_t y = e.y;
+        const uint32_t b = lo & y & 0xffffu;
         a = e.x + (b << 3);
-        const uint32_t k = __byte_perm(e.y, 0, 0x4442);
+        e = lds64(a);
+        const uint32_t k = __byte_perm(y, 0, 0x4442);
         lo = __funnelshift_r(lo, hi, k);
         hi >>= k;
         pos += k;
         if (pos > lim) {
             const uint32_t avail = lim + 32 - pos;   // 16..31
-            const uint32_t u = src(next);
             lo |= u << avail;
             hi = u >> (32 - avail);
             lim += 32;
             ++next;
         }
-        return e.y;
+        return y;
     }
 };
 
