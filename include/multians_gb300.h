@@ -129,6 +129,24 @@ int mans_host_encode(const uint8_t* sym, size_t n, uint32_t L, uint32_t table_se
                      uint32_t* dec_table, uint32_t* units, size_t cap, size_t* n_units,
                      uint32_t* first_bit, uint32_t* first_state);
 
+/* Decode that allocates nothing.  No counterpart in the reference: its
+ * decode needs caller-allocated CUHDGPUDecoderMemory.  For callers that may
+ * not allocate device memory when they decode (inside a host application's
+ * own memory pool, on a path that must not stall behind cudaMalloc/cudaFree,
+ * or when device memory is already exhausted): the workspace is a 32 MiB
+ * device array inside this library (mans_noalloc_scratch_bytes), held by
+ * every GPU that loads the library until exit.  Same arguments and result
+ * as mans_decode_sync; streams whose planned workspace exceeds the array
+ * (about 13 million units at 6 bits/symbol) get MANS_ERR_AUX_SMALL before
+ * any GPU work.  All calls on a device share the array: calls that overlap
+ * on the GPU race, so serialise them.  The first call on a device looks up
+ * the array's address and should come before any stream capture.
+ * Synchronous on `stream`. */
+int mans_decode_noalloc(const uint32_t* d_units, size_t n_units, uint8_t* d_out, size_t n_out,
+                        const uint32_t* d_table, uint32_t L, uint32_t first_state,
+                        uint32_t first_bit, void* stream, uint32_t* status_out);
+size_t mans_noalloc_scratch_bytes(void);
+
 /* Library version string. */
 const char* mans_version(void);
 
