@@ -111,6 +111,42 @@ int mans_timing_collect(float* ms_per_kernel, int n_kernels, int* n_decodes);
 /* Number of kernels launched by the last decode on this thread. */
 uint32_t mans_last_launch_count(void);
 
+/* ---- Batched decode of many independent streams --------------------------
+ * No single counterpart in the reference, which decodes one stream per
+ * CUHDGPUDecoder::decode call (src/main.cc:111-116); this decodes a whole
+ * list of streams, each with its own table, in one launch of each kernel
+ * (a work list spans the streams).  mans_batch_create plans every stream,
+ * uploads the stream parameters and work list once, and uses the caller's
+ * device workspace when given (mans_batch_workspace_size bytes) or
+ * allocates its own.  mans_batch_decode enqueues the decode on `stream`
+ * (nothing allocated, no host synchronisation); mans_batch_graph_decode
+ * captures that into a CUDA graph on first use (on a private stream) and
+ * replays it on `stream`.  Every stream gets its own device status word
+ * (mans_batch_status: OR over the batch and, if per_stream != NULL, one
+ * word per stream). */
+typedef struct {
+    const uint32_t* d_units;  /* 16-byte aligned */
+    uint64_t n_units;
+    uint8_t* d_out;
+    uint64_t n_out;
+    const uint32_t* d_table;
+    uint32_t L;
+    uint32_t first_state;
+    uint32_t first_bit;
+    uint32_t reserved;
+} mans_stream_desc;
+
+typedef struct mans_batch mans_batch;
+
+int mans_batch_workspace_size(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                              size_t* bytes);
+int mans_batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                      void* d_workspace, size_t workspace_bytes, mans_batch** out);
+int mans_batch_decode(mans_batch* b, void* stream);
+int mans_batch_graph_decode(mans_batch* b, void* stream);
+int mans_batch_status(mans_batch* b, void* stream, uint32_t* or_status, uint32_t* per_stream);
+int mans_batch_destroy(mans_batch* b);
+
 /* Host-side data preparation (the reference's ANSTableGenerator +
  * ANSEncoder path, src/ans_table_generator.cc, src/ans_encoder.cc, as C
  * calls).  mans_host_gen_symbols: n seeded symbols

@@ -1,0 +1,98 @@
+"""Batched decode of many independent streams through the C ABI
+(mans_batch_*): one launch of each kernel covers the whole batch, optionally
+replayed as a CUDA graph."""
+from __future__ import annotations
+
+import ctypes
+
+from ._lib import Cfg, MansError, check, lib
+
+
+class StreamDesc(ctypes.Structure):
+    _fields_ = [("d_units", ctypes.c_void_p), ("n_units", ctypes.c_uint64),
+                ("d_out", ctypes.c_void_p), ("n_out", ctypes.c_uint64),
+                ("d_table", ctypes.c_void_p), ("L", ctypes.c_uint32),
+                ("first_state", ctypes.c_uint32), ("first_bit", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+def _sig():
+    L = lib()
+    vp, u32 = ctypes.c_void_p, ctypes.c_uint32
+    L.mans_batch_workspace_size.argtypes = [ctypes.POINTER(StreamDesc), u32, ctypes.POINTER(Cfg),
+                                            ctypes.POINTER(ctypes.c_size_t)]
+    L.mans_batch_workspace_size.restype = ctypes.c_int
+    L.mans_batch_create.argtypes = [ctypes.POINTER(StreamDesc), u32, ctypes.POINTER(Cfg), vp,
+                                    ctypes.c_size_t, ctypes.POINTER(vp)]
+    L.mans_batch_create.restype = ctypes.c_int
+    L.mans_batch_decode.argtypes = [vp, vp]
+    L.mans_batch_decode.restype = ctypes.c_int
+    L.mans_batch_graph_decode.argtypes = [vp, vp]
+    L.mans_batch_graph_decode.restype = ctypes.c_int
+    L.mans_batch_status.argtypes = [vp, vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    L.mans_batch_status.restype = ctypes.c_int
+    L.mans_batch_destroy.argtypes = [vp]
+    L.mans_batch_destroy.restype = ctypes.c_int
+    return L
+
+
+def desc(units, n_units, out, n_out, table, L, first_state, first_bit) -> StreamDesc:
+    """A stream descriptor from CUDA tensors (units/table int32 or uint32 views)."""
+    return StreamDesc(units.data_ptr() if units is not None else None, int(n_units),
+                      out.data_ptr() if out is not None else None, int(n_out),
+                      table.data_ptr() if table is not None else None, int(L),
+                      int(first_state), int(first_bit), 0)
+
+
+class Batch:
+    """A planned batch; decode() enqueues it, graph_decode() replays it as a
+    CUDA graph, status() returns (or-status, per-stream statuses)."""
+
+    def __init__(self, descs, hint: dict | None = None, workspace=None):
+        self._L = _sig()
+        self.n = len(descs)
+        arr = (StreamDesc * self.n)(*descs)
+        self._descs = arr
+        h = Cfg(**hint) if hint else None
+        handle = ctypes.c_void_p(0)
+        ws_ptr = ctypes.c_void_p(workspace.data_ptr()) if workspace is not None else None
+        ws_bytes = workspace.numel() if workspace is not None else 0
+        check(self._L.mans_batch_create(arr, self.n, ctypes.byref(h) if h else None, ws_ptr,
+                                        ws_bytes, ctypes.byref(handle)), "mans_batch_create")
+        self.handle = handle
+
+    @staticmethod
+    def workspace_size(descs, hint: dict | None = None) -> int:
+        L = _sig()
+        arr = (StreamDesc * len(descs))(*descs)
+        h = Cfg(**hint) if hint else None
+        out = ctypes.c_size_t(0)
+        check(L.mans_batch_workspace_size(arr, len(descs), ctypes.byref(h) if h else None,
+                                          ctypes.byref(out)), "mans_batch_workspace_size")
+        return int(out.value)
+
+    def decode(self, stream) -> None:
+        check(self._L.mans_batch_decode(self.handle, ctypes.c_void_p(stream.cuda_stream)),
+              "mans_batch_decode")
+
+    def graph_decode(self, stream) -> None:
+        check(self._L.mans_batch_graph_decode(self.handle, ctypes.c_void_p(stream.cuda_stream)),
+              "mans_batch_graph_decode")
+
+    def status(self, stream):
+        acc = ctypes.c_uint32(0)
+        per = (ctypes.c_uint32 * self.n)()
+        check(self._L.mans_batch_status(self.handle, ctypes.c_void_p(stream.cuda_stream),
+                                        ctypes.byref(acc), per), "mans_batch_status")
+        return int(acc.value), [int(x) for x in per]
+
+    def close(self) -> None:
+        if self.handle:
+            self._L.mans_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

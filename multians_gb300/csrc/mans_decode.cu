@@ -38,6 +38,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <vector>
 
 #include "mans_device.cuh"
 #include "mans_tma.cuh"
@@ -58,6 +59,8 @@ struct DecodeParams {
     unsigned long long* Mpre;   // [nreg] prefix max of m
     long long* Dpre;            // [nreg] prefix sum of delta
     uint32_t* status;
+    struct ScanTile* scan_tiles;   // [ntiles] look-back records
+    uint32_t* scan_flags;          // [ntiles] look-back flags, then the tile ticket
     unsigned long long n_out;
     uint32_t n_units;
     uint32_t L;
@@ -78,7 +81,7 @@ struct DecodeParams {
 // every entry is a zero-bit self loop is a single-symbol table and sets
 // MANS_DEV_DEGENERATE.  Zero-bit runs are folded by pointer doubling over
 // the run-successor links (runs are strictly decreasing, so they end).
-__global__ void k_prep(DecodeParams p) {
+__device__ __forceinline__ void prep_body(const DecodeParams& p) {
     extern __shared__ uint32_t sm[];
     const uint32_t L = p.L;
     uint32_t* plain = sm;                        // base | k << 16 | sym << 24
@@ -142,6 +145,8 @@ __global__ void k_prep(DecodeParams p) {
     }
 }
 
+__global__ void k_prep(DecodeParams p) { prep_body(p); }
+
 __device__ __forceinline__ uint2 make_rec(uint32_t rel, uint32_t idx, uint32_t cnt) {
     return make_uint2(rel | (idx << 8), cnt);
 }
@@ -165,6 +170,7 @@ constexpr uint32_t kRingStride = kRingUnits * 4 + 16;   // bytes per lane (padde
 constexpr uint32_t kRelease = 4;
 constexpr uint32_t kSyncThreads = 64;
 constexpr uint32_t kMaxBlockUnits = 16;
+constexpr uint32_t kMaxWalkSlots = 8;
 
 enum : uint32_t { kModeG = 0, kModeWalk = 1, kModeDone = 2 };
 
@@ -182,7 +188,7 @@ __device__ __forceinline__ void ring_fill(uint32_t slot_addr, const uint32_t* __
     }
 }
 
-__global__ void __launch_bounds__(kSyncThreads) k_sync(DecodeParams p) {
+__device__ __forceinline__ void sync_body(const DecodeParams& p, uint32_t rbase) {
     extern __shared__ __align__(16) uint2 s_tab[];
     load_prepared(s_tab, p.tab_sync, p.L);
     if (*(volatile uint32_t*) p.status & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE)) return;
@@ -191,13 +197,13 @@ __global__ void __launch_bounds__(kSyncThreads) k_sync(DecodeParams p) {
     const uint32_t tab_bytes = (p.L * 8 + 15) & ~15u;
     const uint32_t ring = tb + tab_bytes + threadIdx.x * kRingStride;
     const uint32_t bars = tb + tab_bytes + blockDim.x * kRingStride + warp * 40;  // 5 mbarriers
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t k = rbase + threadIdx.x;
     const uint32_t* __restrict__ in = p.units;
     const uint32_t n = p.n_units;
     const uint32_t Bbits = p.B * 32;
     const UnitSrc rs{ring, 0u, kRingUnits - 1, kRingUnits - 1};
 
-    if ((blockIdx.x * blockDim.x + (warp << 5)) >= p.nreg) return;   // whole warp idle
+    if ((rbase + (warp << 5)) >= p.nreg) return;   // whole warp idle
     if (lane == 0) {
         for (uint32_t i = 0; i < 5; ++i) mbar_init(bars + 8 * i, 1);
         fence_mbar_init();
@@ -325,6 +331,10 @@ __global__ void __launch_bounds__(kSyncThreads) k_sync(DecodeParams p) {
     if (timed_out) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
 }
 
+__global__ void __launch_bounds__(kSyncThreads) k_sync(DecodeParams p) {
+    sync_body(p, blockIdx.x * blockDim.x);
+}
+
 // Exclusive prefix max of m (identity 0) and prefix sum of delta over the
 // regions: single-pass decoupled look-back.  Tiles of kScanTile regions are
 // taken in launch order through an atomic ticket, so a tile only ever waits
@@ -341,17 +351,14 @@ struct ScanTile {               // one per tile, 32 bytes
     long long inc_s;            // inclusive prefix sum
 };
 
-__global__ void __launch_bounds__(kScanThreads) k_scan(DecodeParams p, ScanTile* tiles,
-                                                      uint32_t* flags, uint32_t* ticket) {
+__device__ __forceinline__ void scan_body(const DecodeParams& p, uint32_t tile) {
     __shared__ unsigned long long s_m[kScanThreads];
     __shared__ long long s_s[kScanThreads];
-    __shared__ uint32_t s_tile;
     __shared__ unsigned long long s_pm;
     __shared__ long long s_ps;
+    ScanTile* tiles = p.scan_tiles;
+    uint32_t* flags = p.scan_flags;
     const uint32_t t = threadIdx.x;
-    if (t == 0) s_tile = atomicAdd(ticket, 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
     const uint32_t base = tile * kScanTile + t * kScanPer;
     unsigned long long vm[kScanPer];
     long long vs[kScanPer];
@@ -436,6 +443,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DecodeParams p, ScanTile*
     }
 }
 
+// Tiles are taken in launch order through an atomic ticket (the word after
+// the flags), so a tile only waits on tiles that have already started.
+__global__ void __launch_bounds__(kScanThreads) k_scan(DecodeParams p) {
+    __shared__ uint32_t s_tile;
+    if (threadIdx.x == 0) s_tile = atomicAdd(p.scan_flags + (p.nreg + kScanTile - 1) / kScanTile, 1u);
+    __syncthreads();
+    scan_body(p, s_tile);
+}
+
 // Entry (bit offset from the block start, state index) and global output
 // offset of block b.  Returns false when no trajectory owns the block (a
 // walk ran out of slots).
@@ -473,15 +489,15 @@ __device__ __forceinline__ void sts8(uint32_t a, uint32_t v) {
     asm volatile("st.shared.u8 [%0], %1;" :: "r"(a), "r"(v) : "memory");
 }
 
-__global__ void __launch_bounds__(kFinalThreads) k_final(DecodeParams p) {
+__device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, uint32_t nctas) {
     extern __shared__ __align__(16) uint2 s_tab[];
     load_prepared(s_tab, p.tab_sym, p.L);
     const uint32_t st = *(volatile uint32_t*) p.status;
     if (st & MANS_DEV_DEGENERATE) {
         // single-symbol table: every state decodes that symbol
         const uint8_t sym = (uint8_t) (__ldg(p.table) >> 16);
-        const unsigned long long stride = (unsigned long long) gridDim.x * blockDim.x;
-        for (unsigned long long i = (unsigned long long) blockIdx.x * blockDim.x + threadIdx.x;
+        const unsigned long long stride = (unsigned long long) nctas * blockDim.x;
+        for (unsigned long long i = (unsigned long long) cta * blockDim.x + threadIdx.x;
              i < p.n_out; i += stride)
             p.out[i] = sym;
         return;
@@ -499,7 +515,7 @@ __global__ void __launch_bounds__(kFinalThreads) k_final(DecodeParams p) {
     const uint32_t bar = wbase + 32 * tile_stride;       // 16 bytes reserved
     const uint32_t stage_addr = bar + 16;
 
-    const uint32_t b0 = blockIdx.x * blockDim.x + (warp << 5);
+    const uint32_t b0 = cta * blockDim.x + (warp << 5);
     if (b0 >= p.nblk) return;
     const uint32_t b = b0 + lane;
     const bool have = b < p.nblk;
@@ -603,6 +619,68 @@ __global__ void __launch_bounds__(kFinalThreads) k_final(DecodeParams p) {
     for (uint32_t v = lane; v < nvec; v += 32) dst[v] = src[v];
 }
 
+__global__ void __launch_bounds__(kFinalThreads) k_final(DecodeParams p) {
+    final_body(p, blockIdx.x, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
+// Batched launches: every CTA takes one work item {stream, first region /
+// tile / CTA index} from a host-built list and the parameters of its stream
+// from the stream table, so one launch of each kernel covers every stream
+// of the batch.
+
+struct BatchItem {
+    uint32_t stream;
+    uint32_t index;    // first region (sync), tile (scan) or CTA of the stream (final)
+    uint32_t count;    // CTAs the stream has in this launch (final)
+    uint32_t pad;
+};
+
+__device__ __forceinline__ void load_params(DecodeParams& dst, const DecodeParams* src) {
+    static_assert(sizeof(DecodeParams) % 4 == 0, "word copy");
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+    uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
+    for (uint32_t i = threadIdx.x; i < sizeof(DecodeParams) / 4; i += blockDim.x) d[i] = s[i];
+    __syncthreads();
+}
+
+__global__ void k_prep_batch(const DecodeParams* ps) {
+    __shared__ DecodeParams sp;
+    load_params(sp, ps + blockIdx.x);
+    prep_body(sp);
+}
+
+__global__ void __launch_bounds__(kSyncThreads) k_sync_batch(const DecodeParams* ps,
+                                                             const BatchItem* items) {
+    __shared__ DecodeParams sp;
+    const BatchItem it = items[blockIdx.x];
+    load_params(sp, ps + it.stream);
+    sync_body(sp, it.index);
+}
+
+// The batch ticket hands out items in list order; the list holds each
+// stream's tiles in increasing order, so a tile only waits on tiles of its
+// own stream that have already started.
+__global__ void __launch_bounds__(kScanThreads) k_scan_batch(const DecodeParams* ps,
+                                                             const BatchItem* items,
+                                                             uint32_t* ticket) {
+    __shared__ DecodeParams sp;
+    __shared__ uint32_t s_item;
+    if (threadIdx.x == 0) s_item = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const BatchItem it = items[s_item];
+    load_params(sp, ps + it.stream);
+    scan_body(sp, it.index);
+}
+
+__global__ void __launch_bounds__(kFinalThreads) k_final_batch(const DecodeParams* ps,
+                                                               const BatchItem* items) {
+    __shared__ DecodeParams sp;
+    const BatchItem it = items[blockIdx.x];
+    load_params(sp, ps + it.stream);
+    final_body(sp, it.index, it.count);
+}
+
 // ---------------------------------------------------------------------------
 // host side
 
@@ -685,16 +763,28 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
         c.block_units = std::min<uint32_t>(std::max<uint32_t>(pow2_floor(std::max<uint64_t>(b, 1)), 4), 256);
     }
     c.block_units = std::min<uint32_t>(std::max<uint32_t>(c.block_units & ~3u, 4), kMaxBlockUnits);
+    // Sync walks: a walk runs from a region's end until its trajectory meets
+    // the next region's guessed one, crossing up to walk_slots regions.  The
+    // meeting distance grows with L; measured on the generator's data its
+    // tail stays below about 1.5 L units, so regions and slots are sized for
+    // R * (slots - 1) >= 2 L.
+    const uint64_t tail = std::max<uint64_t>(256, 2ull * L);
+    const uint64_t r_min = (tail + kMaxWalkSlots - 2) / (kMaxWalkSlots - 1);
     if (c.region_blocks == 0) {
         uint64_t R = L <= 1024 ? 512 : 2048;  // units per sync region
         // keep at least ~4 regions per SM when the stream is small
         const uint64_t want_regions = 152ull * 4;
-        while (R > 64 && n_units / R < want_regions) R /= 2;
+        while (R > r_min && n_units / R < want_regions) R /= 2;
+        R = std::max<uint64_t>(R, std::min<uint64_t>(r_min, 8ull * c.block_units));
+        R = std::max<uint64_t>(R, r_min);
         // an odd block count keeps lanes of a warp (one region each) off
         // power-of-two strides, which would pile them into the same L1 sets
-        c.region_blocks = (uint32_t) std::max<uint64_t>(1, R / c.block_units) | 1u;
+        c.region_blocks = (uint32_t) std::max<uint64_t>(8, R / c.block_units) | 1u;
     }
-    if (c.walk_slots == 0) c.walk_slots = 4;
+    if (c.walk_slots == 0) {
+        const uint64_t R = (uint64_t) c.region_blocks * c.block_units;
+        c.walk_slots = (uint32_t) std::min<uint64_t>(kMaxWalkSlots, std::max<uint64_t>(2, (tail + R - 1) / R + 1));
+    }
     if (c.threads == 0) c.threads = 128;
     c.threads = std::min<uint32_t>(128, std::max<uint32_t>(32, c.threads & ~31u));
     *out = c;
@@ -710,8 +800,8 @@ size_t mans_aux_size(size_t n_units, const mans_cfg* cfg) {
 }
 
 size_t mans_aux_size_max(size_t n_units) {
-    // smallest blocks (4 units), smallest regions (64 units), 8 slots
-    mans_cfg c = {4, 16, 8, 128};
+    // smallest blocks (4 units), fewest blocks per region (8), most slots
+    mans_cfg c = {4, 8, kMaxWalkSlots, 128};
     return mans_aux_size(n_units, &c);
 }
 
@@ -767,6 +857,8 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     p.status = (uint32_t*) (base + lay.status);
     p.tab_sync = (uint2*) (base + lay.tab_sync);
     p.tab_sym = (uint2*) (base + lay.tab_sym);
+    p.scan_tiles = (ScanTile*) (base + lay.scan_tiles);
+    p.scan_flags = (uint32_t*) (base + lay.scan_flags);
     p.n_out = n_out;
     p.n_units = (uint32_t) n_units;
     p.L = L;
@@ -805,9 +897,7 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     timing_mark(1, st);
     k_sync<<<(unsigned) ((nreg + kSyncThreads - 1) / kSyncThreads), kSyncThreads, smem_sync, st>>>(p);
     timing_mark(2, st);
-    k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(
-        p, (ScanTile*) (base + lay.scan_tiles), (uint32_t*) (base + lay.scan_flags),
-        (uint32_t*) (base + lay.scan_flags) + ntiles);
+    k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(p);
     timing_mark(3, st);
     k_final<<<(unsigned) ((nblk + kFinalThreads - 1) / kFinalThreads), kFinalThreads, smem_final, st>>>(p);
     timing_mark(4, st);
@@ -893,6 +983,270 @@ int mans_decode_sync(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     if (st & MANS_DEV_BAD_TABLE) return MANS_ERR_TABLE;
     if (st & MANS_DEV_SYNC_OVERFLOW) return MANS_ERR_SYNC;
     if (st & MANS_DEV_SCAN_TIMEOUT) return MANS_ERR_CUDA;
+    return MANS_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// Batched decode of many independent streams (one launch of each kernel for
+// the whole batch; see the BatchItem kernels above).
+
+}  // extern "C"
+
+namespace mans {
+
+struct BatchStreamPlan {
+    mans_cfg cfg;
+    size_t nblk, nreg, ntiles;
+    size_t data_off;     // offset of this stream's slice in the data region
+    size_t flags_off;    // word offset of its scan flags in the flag array
+    uint32_t stage_cap;
+    bool active;
+};
+
+struct BatchLayout {
+    size_t status, flags, ticket, params, items, data, total;
+    size_t n_sync, n_scan, n_final, n_items;
+    size_t smem_sync, smem_final, smem_prep;
+};
+
+static size_t stream_data_bytes(const BatchStreamPlan& sp) {
+    const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots);
+    return a.total;
+}
+
+static uint32_t stage_cap_for(double per_unit, uint32_t B) {
+    uint64_t cap = (uint64_t) (per_unit * 32.0 * B * 1.5) + 256;
+    cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
+    return (uint32_t) ((cap + 15) & ~(uint64_t) 15);
+}
+
+static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hint,
+                      std::vector<BatchStreamPlan>& plans, BatchLayout& lay) {
+    plans.assign(n, BatchStreamPlan{});
+    size_t data = 0, flag_words = 0;
+    lay.n_sync = lay.n_scan = lay.n_final = 0;
+    lay.smem_sync = lay.smem_final = lay.smem_prep = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        BatchStreamPlan& sp = plans[i];
+        sp.active = d[i].n_out > 0;
+        if (!sp.active) continue;
+        if (!d[i].d_units || !d[i].d_out || !d[i].d_table || d[i].n_units == 0 ||
+            d[i].n_units > 0xffffffffull || d[i].L < 2 || d[i].L > kMaxStates ||
+            d[i].first_state < d[i].L || d[i].first_state >= 2 * d[i].L || d[i].first_bit > 32 ||
+            ((uintptr_t) d[i].d_units & 15) != 0)
+            return MANS_ERR_ARG;
+        int rc = mans_plan(d[i].n_units, d[i].n_out, d[i].L, hint, &sp.cfg);
+        if (rc != MANS_OK) return rc;
+        sp.nblk = num_blocks(d[i].n_units, sp.cfg.block_units);
+        sp.nreg = (sp.nblk + sp.cfg.region_blocks - 1) / sp.cfg.region_blocks;
+        sp.ntiles = (sp.nreg + kScanTile - 1) / kScanTile;
+        sp.data_off = data;
+        data += align256(stream_data_bytes(sp));
+        sp.flags_off = flag_words;
+        flag_words += sp.ntiles + 1;
+        sp.stage_cap = stage_cap_for((double) d[i].n_out / (double) d[i].n_units,
+                                     sp.cfg.block_units);
+        lay.n_sync += (sp.nreg + kSyncThreads - 1) / kSyncThreads;
+        lay.n_scan += sp.ntiles;
+        lay.n_final += (sp.nblk + kFinalThreads - 1) / kFinalThreads;
+        const size_t tab = ((size_t) d[i].L * 8 + 15) & ~(size_t) 15;
+        lay.smem_sync = std::max(lay.smem_sync, tab + (size_t) kSyncThreads * kRingStride +
+                                                    (kSyncThreads / 32) * 40);
+        const uint32_t tile_bytes = (sp.cfg.block_units + 4) * 4;
+        const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
+        lay.smem_final = std::max(lay.smem_final,
+                                  tab + (size_t) (kFinalThreads / 32) *
+                                            ((size_t) 32 * tile_stride + 16 + sp.stage_cap + 16));
+        lay.smem_prep = std::max(lay.smem_prep, (size_t) d[i].L * 12);
+    }
+    lay.n_items = lay.n_sync + lay.n_scan + lay.n_final;
+    size_t o = 0;
+    lay.status = o; o += align256((size_t) n * 4);
+    lay.flags = o; o += align256(flag_words * 4);
+    lay.ticket = o; o += 256;
+    lay.params = o; o += align256((size_t) n * sizeof(DecodeParams));
+    lay.items = o; o += align256(lay.n_items * sizeof(BatchItem));
+    lay.data = o; o += data;
+    lay.total = o;
+    return MANS_OK;
+}
+
+}  // namespace mans
+
+struct mans_batch {
+    int device = 0;
+    uint32_t n = 0;
+    char* base = nullptr;        // device workspace
+    bool owns = false;
+    std::vector<mans::BatchStreamPlan> plans;
+    mans::BatchLayout lay{};
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t graph_stream = nullptr;
+};
+
+extern "C" {
+
+int mans_batch_workspace_size(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                              size_t* bytes) {
+    if (!streams || !bytes || n == 0) return MANS_ERR_ARG;
+    std::vector<BatchStreamPlan> plans;
+    BatchLayout lay;
+    int rc = plan_batch(streams, n, hint, plans, lay);
+    if (rc != MANS_OK) return rc;
+    *bytes = lay.total;
+    return MANS_OK;
+}
+
+int mans_batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                      void* d_workspace, size_t workspace_bytes, mans_batch** out) {
+    if (!streams || !out || n == 0) return MANS_ERR_ARG;
+    *out = nullptr;
+    mans_batch* b = new mans_batch();
+    b->n = n;
+    cudaGetDevice(&b->device);
+    int rc = plan_batch(streams, n, hint, b->plans, b->lay);
+    if (rc != MANS_OK) { delete b; return rc; }
+    if (d_workspace) {
+        if (workspace_bytes < b->lay.total) { delete b; return MANS_ERR_AUX_SMALL; }
+        b->base = (char*) d_workspace;
+    } else {
+        if (cudaMalloc(&b->base, b->lay.total) != cudaSuccess) { delete b; return MANS_ERR_NOMEM; }
+        b->owns = true;
+    }
+    // stream parameters and work items, built on the host and uploaded once
+    std::vector<DecodeParams> ps(n);
+    std::vector<BatchItem> items(b->lay.n_items);
+    size_t is = 0, ic = b->lay.n_sync, iff = b->lay.n_sync + b->lay.n_scan;
+    for (uint32_t i = 0; i < n; ++i) {
+        const BatchStreamPlan& sp = b->plans[i];
+        DecodeParams& p = ps[i];
+        std::memset(&p, 0, sizeof(p));
+        p.status = (uint32_t*) (b->base + b->lay.status) + i;
+        if (!sp.active) continue;
+        const mans_stream_desc& d = streams[i];
+        const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots);
+        char* slice = b->base + b->lay.data + sp.data_off;
+        p.units = d.d_units;
+        p.out = d.d_out;
+        p.table = d.d_table;
+        p.tab_sync = (uint2*) (slice + a.tab_sync);
+        p.tab_sym = (uint2*) (slice + a.tab_sym);
+        p.rec_g = (uint2*) (slice + a.rec_g);
+        p.rec_w = (uint2*) (slice + a.rec_w);
+        p.m = (unsigned long long*) (slice + a.m);
+        p.delta = (long long*) (slice + a.delta);
+        p.Mpre = (unsigned long long*) (slice + a.Mpre);
+        p.Dpre = (long long*) (slice + a.Dpre);
+        p.scan_tiles = (ScanTile*) (slice + a.scan_tiles);
+        p.scan_flags = (uint32_t*) (b->base + b->lay.flags) + sp.flags_off;
+        p.n_out = d.n_out;
+        p.n_units = (uint32_t) d.n_units;
+        p.L = d.L;
+        p.first_idx = d.first_state - d.L;
+        p.first_pos = 32 - d.first_bit;
+        p.B = sp.cfg.block_units;
+        p.nb = sp.cfg.region_blocks;
+        p.dmax = sp.cfg.walk_slots;
+        p.nblk = (uint32_t) sp.nblk;
+        p.nreg = (uint32_t) sp.nreg;
+        p.stage_cap = sp.stage_cap;
+        for (size_t r = 0; r < sp.nreg; r += kSyncThreads) items[is++] = {i, (uint32_t) r, 0, 0};
+        for (size_t t = 0; t < sp.ntiles; ++t) items[ic++] = {i, (uint32_t) t, 0, 0};
+        const uint32_t nctas = (uint32_t) ((sp.nblk + kFinalThreads - 1) / kFinalThreads);
+        for (uint32_t c = 0; c < nctas; ++c) items[iff++] = {i, c, nctas, 0};
+    }
+    if (cudaMemcpy(b->base + b->lay.params, ps.data(), n * sizeof(DecodeParams),
+                   cudaMemcpyHostToDevice) != cudaSuccess ||
+        (b->lay.n_items &&
+         cudaMemcpy(b->base + b->lay.items, items.data(), items.size() * sizeof(BatchItem),
+                    cudaMemcpyHostToDevice) != cudaSuccess)) {
+        mans_batch_destroy(b);
+        return MANS_ERR_CUDA;
+    }
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_prep_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+        cudaFuncSetAttribute(k_sync_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+        cudaFuncSetAttribute(k_final_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set = true;
+    }
+    *out = b;
+    return MANS_OK;
+}
+
+int mans_batch_decode(mans_batch* b, void* stream) {
+    if (!b) return MANS_ERR_ARG;
+    cudaStream_t st = (cudaStream_t) stream;
+    const BatchLayout& L = b->lay;
+    if (cudaMemsetAsync(b->base, 0, L.params, st) != cudaSuccess) return MANS_ERR_CUDA;
+    if (L.n_items == 0) return MANS_OK;
+    const DecodeParams* ps = (const DecodeParams*) (b->base + L.params);
+    const BatchItem* items = (const BatchItem*) (b->base + L.items);
+    k_prep_batch<<<b->n, 1024, L.smem_prep, st>>>(ps);
+    if (L.n_sync)
+        k_sync_batch<<<(unsigned) L.n_sync, kSyncThreads, L.smem_sync, st>>>(ps, items);
+    if (L.n_scan)
+        k_scan_batch<<<(unsigned) L.n_scan, kScanThreads, 0, st>>>(
+            ps, items + L.n_sync, (uint32_t*) (b->base + L.ticket));
+    if (L.n_final)
+        k_final_batch<<<(unsigned) L.n_final, kFinalThreads, L.smem_final, st>>>(
+            ps, items + L.n_sync + L.n_scan);
+    g_last_launches = 4;
+    return cudaGetLastError() == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
+}
+
+int mans_batch_graph_decode(mans_batch* b, void* stream) {
+    if (!b) return MANS_ERR_ARG;
+    if (!b->exec) {
+        // capture on a private stream, replay on the caller's (NULL works)
+        if (!b->graph_stream &&
+            cudaStreamCreateWithFlags(&b->graph_stream, cudaStreamNonBlocking) != cudaSuccess)
+            return MANS_ERR_CUDA;
+        if (cudaStreamBeginCapture(b->graph_stream, cudaStreamCaptureModeThreadLocal) !=
+            cudaSuccess)
+            return MANS_ERR_CUDA;
+        const int rc = mans_batch_decode(b, b->graph_stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(b->graph_stream, &g);
+        if (rc != MANS_OK || ce != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return rc != MANS_OK ? rc : MANS_ERR_CUDA;
+        }
+        if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) {
+            cudaGraphDestroy(g);
+            b->exec = nullptr;
+            return MANS_ERR_CUDA;
+        }
+        b->graph = g;
+    }
+    g_last_launches = 4;
+    return cudaGraphLaunch(b->exec, (cudaStream_t) stream) == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
+}
+
+int mans_batch_status(mans_batch* b, void* stream, uint32_t* or_status, uint32_t* per_stream) {
+    if (!b) return MANS_ERR_ARG;
+    std::vector<uint32_t> v(b->n);
+    cudaStream_t st = (cudaStream_t) stream;
+    if (cudaMemcpyAsync(v.data(), b->base + b->lay.status, b->n * 4, cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return MANS_ERR_CUDA;
+    uint32_t acc = 0;
+    for (uint32_t i = 0; i < b->n; ++i) acc |= v[i];
+    if (or_status) *or_status = acc;
+    if (per_stream) std::memcpy(per_stream, v.data(), b->n * 4);
+    return MANS_OK;
+}
+
+int mans_batch_destroy(mans_batch* b) {
+    if (!b) return MANS_OK;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->graph_stream) cudaStreamDestroy(b->graph_stream);
+    if (b->owns && b->base) cudaFree(b->base);
+    delete b;
     return MANS_OK;
 }
 
