@@ -145,6 +145,10 @@ int mans_batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cf
 int mans_batch_decode(mans_batch* b, void* stream);
 int mans_batch_graph_decode(mans_batch* b, void* stream);
 int mans_batch_status(mans_batch* b, void* stream, uint32_t* or_status, uint32_t* per_stream);
+/* Synchronous: re-decodes every stream whose sync walks ran out of slots
+ * (MANS_DEV_SYNC_OVERFLOW) with longer regions inside that stream's own
+ * workspace slice, and updates its status.  Allocates nothing. */
+int mans_batch_fixup(mans_batch* b, void* stream, uint32_t* n_redone);
 int mans_batch_destroy(mans_batch* b);
 
 /* Host-side data preparation (the reference's ANSTableGenerator +

@@ -31,6 +31,8 @@ def _sig():
     L.mans_batch_graph_decode.restype = ctypes.c_int
     L.mans_batch_status.argtypes = [vp, vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
     L.mans_batch_status.restype = ctypes.c_int
+    L.mans_batch_fixup.argtypes = [vp, vp, ctypes.POINTER(u32)]
+    L.mans_batch_fixup.restype = ctypes.c_int
     L.mans_batch_destroy.argtypes = [vp]
     L.mans_batch_destroy.restype = ctypes.c_int
     return L
@@ -85,6 +87,13 @@ class Batch:
         check(self._L.mans_batch_status(self.handle, ctypes.c_void_p(stream.cuda_stream),
                                         ctypes.byref(acc), per), "mans_batch_status")
         return int(acc.value), [int(x) for x in per]
+
+    def fixup(self, stream) -> int:
+        """Re-decodes the streams whose sync walks overflowed; returns how many."""
+        n = ctypes.c_uint32(0)
+        check(self._L.mans_batch_fixup(self.handle, ctypes.c_void_p(stream.cuda_stream),
+                                       ctypes.byref(n)), "mans_batch_fixup")
+        return int(n.value)
 
     def close(self) -> None:
         if self.handle:

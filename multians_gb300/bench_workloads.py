@@ -1,0 +1,173 @@
+"""Batched and served workloads of bench.py.
+
+batched: 4096 independent streams, sizes log-uniform in [4 KB, 4 MB] of
+uint8 symbols, each with its own lambda ~ U[0.01, 1], its own L = 1024
+table and its own encoding.  value = decoded GB/s of one CUDA-graph replay
+of the batched decode over all streams; the same streams through a loop of
+plain per-stream decodes (mans_decode, asynchronous, one stream) are timed
+beside it.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import json
+import os
+import statistics
+import time
+
+import numpy as np
+
+METRIC = "decoded GB/s on 1 GB300 (plain vs batched/served) + %HBM roofline; p50/p99; bit-exact"
+
+
+def _encode_many(specs, threads):
+    from multians_gb300 import host
+
+    def one(sp):
+        seed, lam, n, L = sp
+        return host.make_stream(seed, lam, n, L)
+
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        return list(ex.map(one, specs))
+
+
+def batched_specs(seed: int, count: int = 4096, lo: float = 4096, hi: float = 4 << 20):
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), count)).astype(np.int64)
+    lams = rng.uniform(0.01, 1.0, count)
+    return [(seed * 7919 + i, float(lams[i]), int(sizes[i]), 1024) for i in range(count)]
+
+
+def run_batched(args, ws, rank, local):
+    import torch
+
+    import multians_gb300 as mg
+    from multians_gb300 import batch
+    from multians_gb300.decoder import decode_async
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    count = int(os.environ.get("MANS_BATCH_STREAMS", "4096"))
+    specs = batched_specs(args.seed + rank, count)
+    t0 = time.time()
+    sts = _encode_many(specs, os.cpu_count() or 8)
+    gen_s = time.time() - t0
+    total_sym = sum(st.n for st in sts)
+    total_comp = sum(st.n_units * 4 for st in sts)
+    units = [torch.from_numpy(st.units.view(np.int32)).to(dev) for st in sts]
+    tables = [torch.from_numpy(st.table.view(np.int32)).to(dev) for st in sts]
+    outs = [torch.empty(st.n, dtype=torch.uint8, device=dev) for st in sts]
+    stream = torch.cuda.current_stream(dev)
+
+    # batched decode
+    descs = [batch.desc(u, st.n_units, o, st.n, t, st.L, st.first_state, st.first_bit)
+             for st, u, t, o in zip(sts, units, tables, outs)]
+    b = batch.Batch(descs)
+    for _ in range(max(3, args.warmup)):
+        b.graph_decode(stream)
+    acc, per = b.status(stream)
+    n_overflow = sum(1 for x in per if x & mg.DEV_SYNC_OVERFLOW)
+    n_redone = b.fixup(stream) if n_overflow else 0
+    acc, per = b.status(stream)
+    ok = acc & ~mg.DEV_DEGENERATE == 0
+    for st, o in zip(sts, outs):
+        if not ok:
+            break
+        ok = bool(np.array_equal(o.cpu().numpy()[::-1], st.symbols))
+    steps = max(3, args.steps)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    torch.cuda.synchronize(dev)
+    from bench import ClockSampler
+    with ClockSampler(local) as clk:
+        evs[0].record(stream)
+        for i in range(steps):
+            b.graph_decode(stream)
+            evs[i + 1].record(stream)
+        torch.cuda.synchronize(dev)
+    per_ms = sorted(evs[i].elapsed_time(evs[i + 1]) for i in range(steps))
+    batch_ms = evs[0].elapsed_time(evs[-1]) / steps
+
+    # loop of plain decodes over the same streams (workspaces allocated up front)
+    plans = [mg.plan(st.n_units, st.n, st.L) for st in sts]
+    auxes = [torch.empty(mg.aux_size(st.n_units, p), dtype=torch.uint8, device=dev)
+             for st, p in zip(sts, plans)]
+
+    def loop():
+        for st, u, t, o, p, a in zip(sts, units, tables, outs, plans, auxes):
+            decode_async(u, st.n_units, o, st.n, t, st.L, st.first_state, st.first_bit, a, p,
+                         stream=stream)
+
+    loop()
+    torch.cuda.synchronize(dev)
+    l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    lsteps = 2
+    l0.record(stream)
+    for _ in range(lsteps):
+        loop()
+    l1.record(stream)
+    torch.cuda.synchronize(dev)
+    loop_ms = l0.elapsed_time(l1) / lsteps
+
+    # e2e: host buffers -> device, graph decode, decoded bytes back
+    h_units = [torch.from_numpy(st.units.view(np.int32)).pin_memory() for st in sts]
+    h_out = [torch.empty(st.n, dtype=torch.uint8).pin_memory() for st in sts]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for hu, u in zip(h_units, units):
+        u.copy_(hu, non_blocking=True)
+    b.graph_decode(stream)
+    for o, ho in zip(outs, h_out):
+        ho.copy_(o, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1)
+    if n_overflow:
+        b.fixup(stream)
+        for o, ho in zip(outs, h_out):
+            ho.copy_(o)
+    e2e_ok = all(np.array_equal(ho.numpy()[::-1], st.symbols) for ho, st in zip(h_out, sts))
+    b.close()
+    if rank != 0:
+        return
+    from bench import measured_peaks
+    hbm, kind = measured_peaks()
+    value = ws * total_sym / (batch_ms / 1e3) / 1e9
+    alg = (total_comp + total_sym) / (batch_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": round(batch_ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic",
+        "config": {"workload": f"batched {count} streams log-uniform [4KB,4MB] lambda~U[0.01,1] L=1024",
+                   "n_streams": count, "n_symbols": total_sym, "compressed_bytes": total_comp,
+                   "seed": args.seed, "mode": "one CUDA-graph replay of the batched decode",
+                   "l2": "inputs larger than L2, no flush"},
+        "bit_exact": bool(ok and e2e_ok),
+        "sync_overflow_streams": n_overflow, "streams_redone": n_redone,
+        "latency_ms": {"p50": round(per_ms[len(per_ms) // 2], 4),
+                       "p99": round(per_ms[min(len(per_ms) - 1, int(0.99 * len(per_ms)))], 4)},
+        "loop_of_plain": {"ms": round(loop_ms, 3),
+                          "value": round(total_sym / (loop_ms / 1e3) / 1e9, 3),
+                          "speedup_batched_vs_loop": round(loop_ms / batch_ms, 3)},
+        "roofline": {"bound": "hbm", "kernel": "batched decode (4 kernels)",
+                     "achieved": round(alg, 2), "peak": hbm, "peak_kind": kind, "unit": "GB/s",
+                     "frac": round(alg / hbm, 4), "traffic": None,
+                     "alg_bytes_per_launch": total_comp + total_sym},
+        "cpu_baseline": None,
+        "e2e": {"value": round(ws * total_sym / (e2e_ms / 1e3) / 1e9, 3), "unit": "GB/s",
+                "h2d_bytes_per_step": total_comp, "d2h_bytes_per_step": total_sym,
+                "bit_exact": bool(e2e_ok)},
+        "gpu_launches": 4 * steps,
+        "clocks": clk.summary(),
+        "gen_seconds": round(gen_s, 2),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run(args, ws, rank, local):
+    if args.workload == "batched":
+        return run_batched(args, ws, rank, local)
+    if args.workload == "served":
+        from multians_gb300 import serve_bench
+        return serve_bench.run(args, ws, rank, local)
+    raise ValueError(args.workload)

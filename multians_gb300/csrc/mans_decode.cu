@@ -170,7 +170,7 @@ constexpr uint32_t kRingStride = kRingUnits * 4 + 16;   // bytes per lane (padde
 constexpr uint32_t kRelease = 4;
 constexpr uint32_t kSyncThreads = 64;
 constexpr uint32_t kMaxBlockUnits = 16;
-constexpr uint32_t kMaxWalkSlots = 8;
+constexpr uint32_t kMaxWalkSlots = 12;
 
 enum : uint32_t { kModeG = 0, kModeWalk = 1, kModeDone = 2 };
 
@@ -766,9 +766,10 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
     // Sync walks: a walk runs from a region's end until its trajectory meets
     // the next region's guessed one, crossing up to walk_slots regions.  The
     // meeting distance grows with L; measured on the generator's data its
-    // tail stays below about 1.5 L units, so regions and slots are sized for
-    // R * (slots - 1) >= 2 L.
-    const uint64_t tail = std::max<uint64_t>(256, 2ull * L);
+    // tail passes 1.5 L units about once per thousand regions, so regions and
+    // slots are sized for R * (slots - 1) >= 4 L.  A walk that still runs out
+    // is reported (MANS_DEV_SYNC_OVERFLOW) and redone with longer regions.
+    const uint64_t tail = std::max<uint64_t>(256, 4ull * L);
     const uint64_t r_min = (tail + kMaxWalkSlots - 2) / (kMaxWalkSlots - 1);
     if (c.region_blocks == 0) {
         uint64_t R = L <= 1024 ? 512 : 2048;  // units per sync region
@@ -1223,6 +1224,40 @@ int mans_batch_graph_decode(mans_batch* b, void* stream) {
     }
     g_last_launches = 4;
     return cudaGraphLaunch(b->exec, (cudaStream_t) stream) == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
+}
+
+int mans_batch_fixup(mans_batch* b, void* stream, uint32_t* n_redone) {
+    if (!b) return MANS_ERR_ARG;
+    if (n_redone) *n_redone = 0;
+    cudaStream_t st = (cudaStream_t) stream;
+    std::vector<uint32_t> v(b->n);
+    if (cudaMemcpyAsync(v.data(), b->base + b->lay.status, b->n * 4, cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return MANS_ERR_CUDA;
+    const DecodeParams* dps = (const DecodeParams*) (b->base + b->lay.params);
+    for (uint32_t i = 0; i < b->n; ++i) {
+        if (!(v[i] & MANS_DEV_SYNC_OVERFLOW) || !b->plans[i].active) continue;
+        DecodeParams p;
+        if (cudaMemcpy(&p, dps + i, sizeof(p), cudaMemcpyDeviceToHost) != cudaSuccess)
+            return MANS_ERR_CUDA;
+        const BatchStreamPlan& sp = b->plans[i];
+        char* slice = b->base + b->lay.data + sp.data_off;
+        const size_t slice_bytes = stream_data_bytes(sp);
+        mans_cfg hint = sp.cfg;
+        hint.region_blocks = sp.cfg.region_blocks * 4;   // longer regions, same slots
+        uint32_t dev_status = 0;
+        const int rc = mans_decode_sync(p.units, p.n_units, p.out, p.n_out, p.table, p.L,
+                                        p.first_idx + p.L, 32 - p.first_pos, slice, slice_bytes,
+                                        &hint, stream, &dev_status);
+        if (rc != MANS_OK && rc != MANS_ERR_SYNC) return rc;
+        if (cudaMemcpyAsync(b->base + b->lay.status + 4ull * i, &dev_status, 4,
+                            cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess)
+            return MANS_ERR_CUDA;
+        if (n_redone) ++*n_redone;
+    }
+    return MANS_OK;
 }
 
 int mans_batch_status(mans_batch* b, void* stream, uint32_t* or_status, uint32_t* per_stream) {
