@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-mb", type=float, default=32.0)
+    ap.add_argument("--rate", type=float, default=0.0,
+                    help="served workload: Poisson arrival rate, requests/s (0 = 50000)")
     return ap.parse_args()
 
 

@@ -45,6 +45,10 @@ typedef enum {
 #define MANS_DEV_COUNT_MISMATCH 0x8u   /* final pass disagreed with scan */
 #define MANS_DEV_SCAN_TIMEOUT   0x10u  /* a bounded device wait gave up */
 
+/* The mans_status a decode with these device bits returns
+ * (MANS_DEV_DEGENERATE alone is success: the output is filled). */
+int mans_status_code(uint32_t dev_status);
+
 /* Launch geometry of one decode.  Zero fields are chosen by the built-in
  * autotuner from (L, units, output size). */
 typedef struct {
@@ -142,6 +146,18 @@ int mans_batch_workspace_size(const mans_stream_desc* streams, uint32_t n, const
                               size_t* bytes);
 int mans_batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
                       void* d_workspace, size_t workspace_bytes, mans_batch** out);
+/* Split layout, for callers that keep every stream's decode workspace
+ * next to its own buffers: a small per-launch header
+ * (mans_batch_header_size bytes at d_header) plus one slice per stream
+ * (mans_batch_slice_size bytes, 16-byte aligned, at d_slices[i]).  The
+ * parameters are uploaded asynchronously on `stream`; the host images stay
+ * in the batch object until mans_batch_destroy. */
+int mans_batch_slice_size(const mans_stream_desc* stream, const mans_cfg* hint, size_t* bytes);
+int mans_batch_header_size(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                           size_t* bytes);
+int mans_batch_create_split(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                            void* d_header, size_t header_bytes, void* const* d_slices,
+                            void* stream, mans_batch** out);
 int mans_batch_decode(mans_batch* b, void* stream);
 int mans_batch_graph_decode(mans_batch* b, void* stream);
 int mans_batch_status(mans_batch* b, void* stream, uint32_t* or_status, uint32_t* per_stream);
@@ -150,6 +166,78 @@ int mans_batch_status(mans_batch* b, void* stream, uint32_t* or_status, uint32_t
  * workspace slice, and updates its status.  Allocates nothing. */
 int mans_batch_fixup(mans_batch* b, void* stream, uint32_t* n_redone);
 int mans_batch_destroy(mans_batch* b);
+
+/* Serving loop.  No counterpart in the reference, whose decode is one
+ * blocking call on the default stream (include/cuhd_gpu_decoder.h:22-36).
+ * A server owns one device range of budget_bytes (default 16 GiB, capped at
+ * creation by the free device memory less 1 GiB), a worker thread and
+ * max_inflight CUDA streams.  Tables are added once and stay resident.
+ * mans_server_submit queues requests and returns at once.  The worker admits
+ * queued requests in arrival order while each one's device memory (units,
+ * output, decode workspace) fits the range, copies host inputs in on a copy
+ * stream, and launches everything admitted since the previous launch as one
+ * batch on a free stream; host outputs are copied back behind the batch on
+ * the same stream.  A request whose memory could never fit is completed
+ * with MANS_ERR_NOMEM; bad arguments with MANS_ERR_ARG.
+ * mans_server_poll returns completions (waiting up to wait_us for one).
+ * Host buffers should be page-locked (cudaHostAlloc / cudaHostRegister):
+ * pageable inputs are staged synchronously, pageable outputs are copied
+ * after the batch completes.  Buffers must stay valid until completion. */
+typedef struct mans_server mans_server;
+
+typedef struct {
+    uint64_t budget_bytes;    /* device memory the server may hold; 0 = 16 GiB */
+    uint32_t max_inflight;    /* batches on the GPU at once; 0 = 2 */
+    uint32_t max_batch;       /* requests per launch; 0 = 4096 */
+    uint32_t reserved[2];
+} mans_server_cfg;
+
+#define MANS_REQ_DEVICE_IO 0x1u   /* units / out are caller-owned device memory */
+
+typedef struct {
+    const uint32_t* units;    /* CUHDInputBuffer order; 16-byte aligned if device */
+    uint64_t n_units;
+    uint8_t* out;             /* n_out symbols, decode order */
+    uint64_t n_out;
+    uint32_t table;           /* id from mans_server_add_table */
+    uint32_t first_state;
+    uint32_t first_bit;
+    uint32_t flags;           /* MANS_REQ_* */
+    uint64_t tag;             /* echoed in the completion */
+    uint64_t arrival_ns;      /* mans_server_now_ns clock; 0 = time of submit */
+} mans_request;
+
+typedef struct {
+    uint64_t tag;
+    int32_t status;           /* mans_status */
+    uint32_t dev_status;      /* MANS_DEV_* bits */
+    uint64_t arrival_ns;
+    uint64_t admit_ns;        /* device memory granted, input copy queued */
+    uint64_t done_ns;         /* output in place */
+    uint64_t batch;           /* sequence number of the launch (0 if none) */
+} mans_completion;
+
+typedef struct {
+    uint64_t submitted, completed, failed;
+    uint64_t batches, kernel_launches, streams_redone;
+    uint64_t bytes_in, bytes_out;
+    uint64_t range_bytes, range_peak, range_in_use;
+    uint64_t admission_waits;  /* times the oldest queued request waited for memory */
+    uint64_t largest_batch;
+} mans_server_stats;
+
+int mans_server_create(const mans_server_cfg* cfg, mans_server** out);
+/* Copies an L-word decoder table to the device; it stays until destroy. */
+int mans_server_add_table(mans_server* s, const uint32_t* host_table, uint32_t L, uint32_t* id);
+int mans_server_submit(mans_server* s, const mans_request* reqs, size_t n);
+int mans_server_poll(mans_server* s, mans_completion* out, size_t cap, size_t* n_out,
+                     uint32_t wait_us);
+int mans_server_stats_get(mans_server* s, mans_server_stats* out);
+/* The clock of arrival_ns / done_ns (CLOCK_MONOTONIC, nanoseconds). */
+uint64_t mans_server_now_ns(void);
+/* Finishes the batches in flight, drops requests not yet launched, joins
+ * the worker and frees everything. */
+int mans_server_destroy(mans_server* s);
 
 /* Host-side data preparation (the reference's ANSTableGenerator +
  * ANSEncoder path, src/ans_table_generator.cc, src/ans_encoder.cc, as C

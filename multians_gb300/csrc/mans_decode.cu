@@ -38,6 +38,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "mans_device.cuh"
@@ -691,6 +692,23 @@ struct AuxLayout {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
 
+// Opts the kernels in to large dynamic shared memory, once per device.
+static void set_kernel_attributes() {
+    static std::mutex mu;
+    static uint64_t done = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lock(mu);
+    if (dev < 64 && ((done >> dev) & 1)) return;
+    cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_sync, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_prep_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_sync_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_final_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (dev < 64) done |= 1ull << dev;
+}
+
 static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax) {
     AuxLayout a;
     size_t o = 0;
@@ -876,13 +894,7 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
         cudaMemsetAsync(base + lay.scan_flags, 0, (ntiles + 1) * 4, st) != cudaSuccess)
         return MANS_ERR_CUDA;
     const size_t smem = ((size_t) L * sizeof(uint2) + 15) & ~(size_t) 15;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-        cudaFuncSetAttribute(k_sync, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-        cudaFuncSetAttribute(k_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
-    }
+    set_kernel_attributes();
     // staging per warp: 1.5x the expected symbols of 32 blocks, 16 B rounded
     const double per_unit = (double) n_out / (double) n_units;
     uint64_t cap = (uint64_t) (per_unit * 32.0 * cfg.block_units * 1.5) + 256;
@@ -952,6 +964,13 @@ int mans_aux_status(const void* d_aux, void* stream, uint32_t* status_out) {
     return MANS_OK;
 }
 
+int mans_status_code(uint32_t st) {
+    if (st & MANS_DEV_BAD_TABLE) return MANS_ERR_TABLE;
+    if (st & (MANS_DEV_SYNC_OVERFLOW | MANS_DEV_COUNT_MISMATCH)) return MANS_ERR_SYNC;
+    if (st & MANS_DEV_SCAN_TIMEOUT) return MANS_ERR_CUDA;
+    return MANS_OK;
+}
+
 int mans_decode_sync(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
                      size_t n_out, const uint32_t* d_table, uint32_t L,
                      uint32_t first_state, uint32_t first_bit, void* d_aux,
@@ -981,10 +1000,7 @@ int mans_decode_sync(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
         c.region_blocks = plan.region_blocks * 4;
     }
     if (status_out) *status_out = st;
-    if (st & MANS_DEV_BAD_TABLE) return MANS_ERR_TABLE;
-    if (st & MANS_DEV_SYNC_OVERFLOW) return MANS_ERR_SYNC;
-    if (st & MANS_DEV_SCAN_TIMEOUT) return MANS_ERR_CUDA;
-    return MANS_OK;
+    return mans_status_code(st);
 }
 
 
@@ -1078,10 +1094,15 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
 struct mans_batch {
     int device = 0;
     uint32_t n = 0;
-    char* base = nullptr;        // device workspace
+    char* base = nullptr;        // device workspace (header, then the slices unless split)
     bool owns = false;
     std::vector<mans::BatchStreamPlan> plans;
+    std::vector<char*> slice;    // per-stream data slice
     mans::BatchLayout lay{};
+    // host images of the parameters and work items; kept until destroy so
+    // an asynchronous upload never reads freed memory
+    std::vector<mans::DecodeParams> ps;
+    std::vector<mans::BatchItem> items;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t graph_stream = nullptr;
@@ -1100,8 +1121,39 @@ int mans_batch_workspace_size(const mans_stream_desc* streams, uint32_t n, const
     return MANS_OK;
 }
 
-int mans_batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
-                      void* d_workspace, size_t workspace_bytes, mans_batch** out) {
+int mans_batch_slice_size(const mans_stream_desc* stream, const mans_cfg* hint, size_t* bytes) {
+    if (!stream || !bytes) return MANS_ERR_ARG;
+    std::vector<BatchStreamPlan> plans;
+    BatchLayout lay;
+    int rc = plan_batch(stream, 1, hint, plans, lay);
+    if (rc != MANS_OK) return rc;
+    *bytes = lay.total - lay.data;
+    return MANS_OK;
+}
+
+int mans_batch_header_size(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                           size_t* bytes) {
+    if (!streams || !bytes || n == 0) return MANS_ERR_ARG;
+    std::vector<BatchStreamPlan> plans;
+    BatchLayout lay;
+    int rc = plan_batch(streams, n, hint, plans, lay);
+    if (rc != MANS_OK) return rc;
+    *bytes = lay.data;
+    return MANS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Plans the batch, places each stream's data slice (inside the workspace
+// after the header, or at slices[i]) and uploads the parameters and work
+// items: synchronously when `async` is false, else on `upload` with the
+// host images kept alive in the batch object.
+int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                 void* d_workspace, size_t workspace_bytes, void* const* slices,
+                 cudaStream_t upload, bool async, mans_batch** out) {
+    using namespace mans;
     if (!streams || !out || n == 0) return MANS_ERR_ARG;
     *out = nullptr;
     mans_batch* b = new mans_batch();
@@ -1109,26 +1161,29 @@ int mans_batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cf
     cudaGetDevice(&b->device);
     int rc = plan_batch(streams, n, hint, b->plans, b->lay);
     if (rc != MANS_OK) { delete b; return rc; }
+    const size_t need = slices ? b->lay.data : b->lay.total;
     if (d_workspace) {
-        if (workspace_bytes < b->lay.total) { delete b; return MANS_ERR_AUX_SMALL; }
+        if (workspace_bytes < need) { delete b; return MANS_ERR_AUX_SMALL; }
         b->base = (char*) d_workspace;
     } else {
-        if (cudaMalloc(&b->base, b->lay.total) != cudaSuccess) { delete b; return MANS_ERR_NOMEM; }
+        if (cudaMalloc(&b->base, need) != cudaSuccess) { delete b; return MANS_ERR_NOMEM; }
         b->owns = true;
     }
-    // stream parameters and work items, built on the host and uploaded once
-    std::vector<DecodeParams> ps(n);
-    std::vector<BatchItem> items(b->lay.n_items);
+    b->slice.assign(n, nullptr);
+    b->ps.assign(n, DecodeParams{});
+    b->items.assign(b->lay.n_items, BatchItem{});
     size_t is = 0, ic = b->lay.n_sync, iff = b->lay.n_sync + b->lay.n_scan;
     for (uint32_t i = 0; i < n; ++i) {
         const BatchStreamPlan& sp = b->plans[i];
-        DecodeParams& p = ps[i];
+        DecodeParams& p = b->ps[i];
         std::memset(&p, 0, sizeof(p));
         p.status = (uint32_t*) (b->base + b->lay.status) + i;
         if (!sp.active) continue;
         const mans_stream_desc& d = streams[i];
         const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots);
-        char* slice = b->base + b->lay.data + sp.data_off;
+        char* slice = slices ? (char*) slices[i] : b->base + b->lay.data + sp.data_off;
+        if (!slice || ((uintptr_t) slice & 255) != 0) { mans_batch_destroy(b); return MANS_ERR_ARG; }
+        b->slice[i] = slice;
         p.units = d.d_units;
         p.out = d.d_out;
         p.table = d.d_table;
@@ -1153,28 +1208,49 @@ int mans_batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cf
         p.nblk = (uint32_t) sp.nblk;
         p.nreg = (uint32_t) sp.nreg;
         p.stage_cap = sp.stage_cap;
-        for (size_t r = 0; r < sp.nreg; r += kSyncThreads) items[is++] = {i, (uint32_t) r, 0, 0};
-        for (size_t t = 0; t < sp.ntiles; ++t) items[ic++] = {i, (uint32_t) t, 0, 0};
+        for (size_t r = 0; r < sp.nreg; r += kSyncThreads) b->items[is++] = {i, (uint32_t) r, 0, 0};
+        for (size_t t = 0; t < sp.ntiles; ++t) b->items[ic++] = {i, (uint32_t) t, 0, 0};
         const uint32_t nctas = (uint32_t) ((sp.nblk + kFinalThreads - 1) / kFinalThreads);
-        for (uint32_t c = 0; c < nctas; ++c) items[iff++] = {i, c, nctas, 0};
+        for (uint32_t c = 0; c < nctas; ++c) b->items[iff++] = {i, c, nctas, 0};
     }
-    if (cudaMemcpy(b->base + b->lay.params, ps.data(), n * sizeof(DecodeParams),
-                   cudaMemcpyHostToDevice) != cudaSuccess ||
-        (b->lay.n_items &&
-         cudaMemcpy(b->base + b->lay.items, items.data(), items.size() * sizeof(BatchItem),
-                    cudaMemcpyHostToDevice) != cudaSuccess)) {
+    const size_t pbytes = n * sizeof(DecodeParams), ibytes = b->items.size() * sizeof(BatchItem);
+    bool ok;
+    if (async) {
+        ok = cudaMemcpyAsync(b->base + b->lay.params, b->ps.data(), pbytes,
+                             cudaMemcpyHostToDevice, upload) == cudaSuccess &&
+             (!ibytes || cudaMemcpyAsync(b->base + b->lay.items, b->items.data(), ibytes,
+                                         cudaMemcpyHostToDevice, upload) == cudaSuccess);
+    } else {
+        ok = cudaMemcpy(b->base + b->lay.params, b->ps.data(), pbytes, cudaMemcpyHostToDevice) ==
+                 cudaSuccess &&
+             (!ibytes || cudaMemcpy(b->base + b->lay.items, b->items.data(), ibytes,
+                                    cudaMemcpyHostToDevice) == cudaSuccess);
+    }
+    if (!ok) {
         mans_batch_destroy(b);
         return MANS_ERR_CUDA;
     }
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_prep_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-        cudaFuncSetAttribute(k_sync_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-        cudaFuncSetAttribute(k_final_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
-    }
+    set_kernel_attributes();
     *out = b;
     return MANS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mans_batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                      void* d_workspace, size_t workspace_bytes, mans_batch** out) {
+    return batch_create(streams, n, hint, d_workspace, workspace_bytes, nullptr, nullptr, false,
+                        out);
+}
+
+int mans_batch_create_split(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                            void* d_header, size_t header_bytes, void* const* d_slices,
+                            void* stream, mans_batch** out) {
+    if (!d_header || !d_slices) return MANS_ERR_ARG;
+    return batch_create(streams, n, hint, d_header, header_bytes, d_slices,
+                        (cudaStream_t) stream, true, out);
 }
 
 int mans_batch_decode(mans_batch* b, void* stream) {
@@ -1242,7 +1318,7 @@ int mans_batch_fixup(mans_batch* b, void* stream, uint32_t* n_redone) {
         if (cudaMemcpy(&p, dps + i, sizeof(p), cudaMemcpyDeviceToHost) != cudaSuccess)
             return MANS_ERR_CUDA;
         const BatchStreamPlan& sp = b->plans[i];
-        char* slice = b->base + b->lay.data + sp.data_off;
+        char* slice = b->slice[i];
         const size_t slice_bytes = stream_data_bytes(sp);
         mans_cfg hint = sp.cfg;
         hint.region_blocks = sp.cfg.region_blocks * 4;   // longer regions, same slots
