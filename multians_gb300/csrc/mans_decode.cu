@@ -545,7 +545,9 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
     uint32_t rel = 0, idx = 0;
     unsigned long long off = 0;
     bool ok = have ? block_entry(p, b, rel, idx, off) : true;
-    unsigned long long off_nx = p.n_out;   // offset of block b + 1
+    // offset of block b + 1; the last block runs to the end of the output
+    // (writes stop at n_out), which may lie before or after its start
+    unsigned long long off_nx = max((unsigned long long) p.n_out, off);
     const unsigned long long from_next = __shfl_down_sync(0xffffffffu, off, 1);
     if (lane < 31 && b + 1 < p.nblk) off_nx = from_next;
     if (lane == 31 && b + 1 < p.nblk) {

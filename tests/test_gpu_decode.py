@@ -97,13 +97,15 @@ def test_overflow_replans(mg, oracle_lib):
     assert np.array_equal(got.cpu().numpy()[::-1], st.symbols)
 
 
-def test_short_output_is_bounded(mg, oracle_lib):
-    """An output size below the symbol count writes exactly that prefix."""
+@pytest.mark.parametrize("short", [1, 12_345, 49_000, 49_963, 49_999])
+def test_short_output_is_bounded(mg, oracle_lib, short):
+    """An output size below the symbol count writes exactly that prefix,
+    also when the cut falls among the last blocks of the stream."""
     O = oracle_lib
     st = O.make_stream(seed=9, lam=0.05, n=50_000, L=1024)
     want = O.decode_seq(st)
-    got = _gpu_decode(mg, st, n_out=12_345)
-    assert np.array_equal(got, want[:12_345])
+    got = _gpu_decode(mg, st, n_out=short)
+    assert np.array_equal(got, want[:short])
 
 
 def test_first_bit_zero(mg, oracle_lib):
