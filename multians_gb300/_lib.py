@@ -122,7 +122,7 @@ def table_check(table) -> int:
     return int(lib().mans_table_check(t.ctypes.data_as(_u32p), t.size))
 
 
-KERNELS = ("k_prep", "k_sync", "k_scan", "k_final")
+KERNELS = ("k_prep", "k_gwalk", "k_wwalk", "k_scan", "k_final")
 
 
 def timing_enable(max_decodes: int) -> None:
@@ -131,8 +131,8 @@ def timing_enable(max_decodes: int) -> None:
 
 def timing_collect() -> tuple[dict, int]:
     """Summed milliseconds per kernel over the decodes timed since
-    timing_enable, and the number of decodes."""
-    buf = (ctypes.c_float * 4)()
+    timing_enable, and the number of decodes (k_wwalk: its three passes)."""
+    buf = (ctypes.c_float * len(KERNELS))()
     n = ctypes.c_int(0)
-    check(lib().mans_timing_collect(buf, 4, ctypes.byref(n)), "mans_timing_collect")
+    check(lib().mans_timing_collect(buf, len(KERNELS), ctypes.byref(n)), "mans_timing_collect")
     return {k: float(buf[i]) for i, k in enumerate(KERNELS)}, int(n.value)

@@ -5,20 +5,22 @@
 // Geometry.  The stream is cut into blocks of B units (final-pass work
 // items) and regions of nb blocks (sync work items, R = nb * B units).
 //
-//  k_sync   one thread per region k.  It decodes region k from a guessed
+//  k_gwalk  one thread per region k.  It decodes region k from a guessed
 //           start (bit 0 of the region, state = the stream's first state;
 //           region 0 starts from the true start), the trajectory Gamma_k,
 //           and records for every block of the region the first codeword
 //           at or after the block start and Gamma_k's symbol count before
-//           it.  It then keeps walking Gamma_k past the region end while
-//           replaying Gamma_{k+1} (region k+1 from its guessed start) until
-//           the two trajectories meet at the same bit position in the same
+//           it, and Gamma_k's entry at the first block of region k + 1.
+//  k_wwalk  (three passes) keeps walking Gamma_k past its region end,
+//           comparing it at every block start with Gamma_{k+1}, until the
+//           two trajectories meet at the same bit position in the same
 //           state: the merge point m_k.  Gamma_k's count minus
 //           Gamma_{k+1}'s count at m_k is delta_k.  Blocks the walk crosses
 //           before m_k get Gamma_k's records in walk slot (region - k).
-//           This is the reference's sync extension
-//           (src/multians_gpu_decoder.cu:251-261, 363-466) with the check
-//           made at every codeword instead of at subsequence ends.
+//           Together these are the reference's guessed-state decode and
+//           sync extension (src/multians_gpu_decoder.cu:195-361, 363-466),
+//           with the check made at every block start instead of at
+//           subsequence ends and with no host round trip per pass.
 //  k_scan   M_k = max(0, m_0..m_{k-1}) and D_k = sum(delta_0..delta_{k-1}).
 //           After M_k the true trajectory is Gamma_k and its global symbol
 //           index is D_k + Gamma_k's count (by induction from Gamma_0,
@@ -61,6 +63,7 @@ struct DecodeParams {
     long long* Dpre;            // [nreg] prefix sum of delta
     uint32_t* status;
     struct ScanTile* scan_tiles;   // [ntiles] look-back records
+    struct WJob* walk_jobs;        // [2][nreg] merge-walk job lists
     uint32_t* scan_flags;          // [ntiles] look-back flags, then the tile ticket
     unsigned long long n_out;
     uint32_t n_units;
@@ -152,18 +155,20 @@ __device__ __forceinline__ uint2 make_rec(uint32_t rel, uint32_t idx, uint32_t c
     return make_uint2(rel | (idx << 8), cnt);
 }
 
-// k_sync staging: every lane owns a ring of kRingSlots chunks of kChunk
-// units in shared memory, filled by TMA bulk copies.  The warp works in
-// rounds; in one round every lane advances its cursor(s) to the next block
-// start (at most kMaxBlockUnits units plus a step).  Between rounds each
-// lane releases its oldest chunk w once its cursors have loaded past unit
-// 32(w+1) + kRelease (a cursor re-started at a block start may re-read up
-// to 3 units behind the other's load point) and refills that slot with
-// chunk w + 4.  Reads stay inside chunks w and w + 1 (the two walk cursors
-// start a round at most one step apart, so a round reads below
-// 32(w+1) + kRelease + 3 + kMaxBlockUnits + 2 < 32(w+2)), so a chunk
-// copied in round r is first read in round r + 2 and round r waits only
-// for the copies of round r - 2.
+// Scan tiling (k_scan): regions per tile.  The word after the tiles' flags
+// is the scan ticket, the next two count the merge-walk job lists.
+constexpr uint32_t kScanThreads = 256;
+constexpr uint32_t kScanPer = 8;
+constexpr uint32_t kScanTile = kScanThreads * kScanPer;
+
+// Sync stage, G pass (k_gwalk): every lane owns a ring of kRingSlots chunks
+// of kChunk units in shared memory, filled by TMA bulk copies.  The warp
+// works in rounds; in one round every lane advances its cursor to the next
+// block start (at most kMaxBlockUnits units plus a step).  Between rounds
+// each lane releases its oldest chunk w once its cursor has loaded past
+// unit 32(w+1) + kRelease and refills that slot with chunk w + 4.  Reads
+// stay inside chunks w and w + 1, so a chunk copied in round r is first
+// read in round r + 2 and round r waits only for the copies of round r - 2.
 constexpr uint32_t kChunk = 32;                    // units per ring slot
 constexpr uint32_t kRingSlots = 4;
 constexpr uint32_t kRingUnits = kChunk * kRingSlots;
@@ -172,8 +177,6 @@ constexpr uint32_t kRelease = 4;
 constexpr uint32_t kSyncThreads = 64;
 constexpr uint32_t kMaxBlockUnits = 16;
 constexpr uint32_t kMaxWalkSlots = 12;
-
-enum : uint32_t { kModeG = 0, kModeWalk = 1, kModeDone = 2 };
 
 __device__ __forceinline__ void ring_fill(uint32_t slot_addr, const uint32_t* __restrict__ in,
                                           uint32_t n, uint32_t chunk, uint32_t bar,
@@ -189,7 +192,11 @@ __device__ __forceinline__ void ring_fill(uint32_t slot_addr, const uint32_t* __
     }
 }
 
-__device__ __forceinline__ void sync_body(const DecodeParams& p, uint32_t rbase) {
+// One lane per region k: decode Gamma_k over the region's blocks, record
+// every block's entry (rec_g) and, for k + 1 < nreg, Gamma_k's entry at the
+// first block of region k + 1 (walk slot 0 of that block), where the merge
+// walk of k_wwalk starts.  Every lane does the same amount of work.
+__device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase) {
     extern __shared__ __align__(16) uint2 s_tab[];
     load_prepared(s_tab, p.tab_sync, p.L);
     if (*(volatile uint32_t*) p.status & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE)) return;
@@ -211,7 +218,7 @@ __device__ __forceinline__ void sync_body(const DecodeParams& p, uint32_t rbase)
     }
     __syncwarp();
 
-    uint32_t mode = k < p.nreg ? kModeG : kModeDone;
+    bool active = k < p.nreg;
     const uint32_t b0 = min(k * p.nb, p.nblk);
     const uint32_t b1 = min(b0 + p.nb, p.nblk);
     const uint64_t origin = (uint64_t) b0 * Bbits;
@@ -222,7 +229,7 @@ __device__ __forceinline__ void sync_body(const DecodeParams& p, uint32_t rbase)
     // initial fill: chunks w .. w+3, completion on barrier 4
     {
         uint32_t mine = 0;
-        if (mode != kModeDone) {
+        if (active) {
             fence_proxy_async();
             for (uint32_t i = 0; i < kRingSlots; ++i) {
                 uint32_t by;
@@ -240,85 +247,51 @@ __device__ __forceinline__ void sync_body(const DecodeParams& p, uint32_t rbase)
         __syncwarp();
     }
 
-    SCursor A, G;
-    uint32_t ca = 0, cg = 0;
-    uint32_t b = b0;        // G: block being decoded; walk: block start to reach
+    SCursor A;
+    uint32_t ca = 0;
+    uint32_t b = b0;        // block being decoded
     uint32_t bs = 0;        // relative start bit of block b
-    uint32_t d = 1, next_region = 0;
-    if (mode == kModeG) {
+    if (active) {
         A.init(rs, origin, start, tb + 8u * p.first_idx);
         p.rec_g[b0] = make_rec(A.pos, entry_index(A.a, tb), 0);
-        if (b0 == b1) mode = kModeDone;
+        if (b0 == b1) active = false;
     }
 
     uint32_t r = 0;
-    while (__any_sync(0xffffffffu, mode != kModeDone)) {
+    while (__any_sync(0xffffffffu, active)) {
         // refill: wait for round r-2's copies, then issue this round's
         if (r >= 2 && !mbar_wait(bars + 8 * ((r - 2) & 3), ((r - 2) >> 2) & 1)) {
             timed_out = true;
             mbar_wait(bars + 8 * ((r - 2) & 3), ((r - 2) >> 2) & 1);
         }
         uint32_t mine = 0;
-        if (mode != kModeDone) {
-            const uint32_t lowest = mode == kModeWalk ? min(A.next, G.next) : A.next;
-            if (lowest >= (w + 1) * kChunk + kRelease) {
-                fence_proxy_async();
-                ring_fill(ring + (w & (kRingSlots - 1)) * kChunk * 4, in, n, w + kRingSlots,
-                          bars + 8 * (r & 3), mine);
-                ++w;
-            }
+        if (active && A.next >= (w + 1) * kChunk + kRelease) {
+            fence_proxy_async();
+            ring_fill(ring + (w & (kRingSlots - 1)) * kChunk * 4, in, n, w + kRingSlots,
+                      bars + 8 * (r & 3), mine);
+            ++w;
         }
         const uint32_t total = __reduce_add_sync(0xffffffffu, mine);
         if (lane == 0) mbar_arrive_expect_tx(bars + 8 * (r & 3), total);
         ++r;
 
-        if (mode == kModeG) {
+        if (active) {
             // decode to the end of block b, record block b+1's entry
             const uint32_t be = bs + Bbits;
             while (A.pos < be) ca += A.step(rs) >> 24;
             ++b;
             bs = be;
+            const uint2 rec = make_rec(A.pos - bs, entry_index(A.a, tb), ca);
             if (b < b1) {
-                p.rec_g[b] = make_rec(A.pos - bs, entry_index(A.a, tb), ca);
-            } else if (k + 1 >= p.nreg) {
-                p.m[k] = ~0ull;
-                p.delta[k] = 0;
-                mode = kModeDone;
+                p.rec_g[b] = rec;
             } else {
-                // walk Gamma_k (A) against a replay of Gamma_{k+1} (G)
-                G.init(rs, origin, (uint64_t) b1 * Bbits, tb + 8u * p.first_idx);
-                next_region = b1 + p.nb;
-                mode = kModeWalk;
-            }
-        }
-        if (mode == kModeWalk) {
-            // both cursors are at (or past) the start of block b
-            while (A.pos < bs || G.pos < bs) {
-                if (A.pos < bs) ca += A.step(rs) >> 24;
-                if (G.pos < bs) cg += G.step(rs) >> 24;
-            }
-            p.rec_w[(size_t) b * p.dmax + (d - 1)] = make_rec(A.pos - bs, entry_index(A.a, tb), ca);
-            if (A.pos == G.pos && A.a == G.a) {
-                p.m[k] = origin + A.pos;
-                p.delta[k] = (long long) ca - (long long) cg;
-                mode = kModeDone;
-            } else {
-                ++b;
-                bs += Bbits;
-                if (b >= p.nblk) {
-                    p.m[k] = ~0ull;   // no merge before the stream end
+                if (k + 1 < p.nreg) {
+                    p.rec_w[(size_t) b1 * p.dmax] = rec;
+                } else {
+                    p.m[k] = ~0ull;   // the last region has no successor
                     p.delta[k] = 0;
-                    mode = kModeDone;
-                } else if (b == next_region) {
-                    ++d;
-                    next_region += p.nb;
-                    if (d > p.dmax) {
-                        atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
-                        p.m[k] = ~0ull;
-                        p.delta[k] = 0;
-                        mode = kModeDone;
-                    }
                 }
+                active = false;
             }
         }
     }
@@ -332,8 +305,193 @@ __device__ __forceinline__ void sync_body(const DecodeParams& p, uint32_t rbase)
     if (timed_out) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
 }
 
-__global__ void __launch_bounds__(kSyncThreads) k_sync(DecodeParams p) {
-    sync_body(p, blockIdx.x * blockDim.x);
+__global__ void __launch_bounds__(kSyncThreads) k_gwalk(DecodeParams p) {
+    gwalk_body(p, blockIdx.x * blockDim.x);
+}
+
+// Sync stage, merge walks (k_wwalk): region k's walk continues Gamma_k from
+// the first block of region k + 1 and stops at the first block start where
+// it meets Gamma_{k+1}: inside region k + 1 Gamma_{k+1} is known from its
+// block records (rec_g), so one cursor suffices; past region k + 1 a second
+// cursor replays Gamma_{k+1} from its entry at region k + 2 (walk slot 0 of
+// that block, written by region k + 1's G pass).  Walks are short on
+// average but their lengths vary a lot, so they run in passes: each lane
+// stages a window of kWindowUnits units (plus 4 of look-ahead) with one
+// TMA copy and walks at most that window per round; a pass allows
+// `max_windows` rounds, and walks still open after that are appended to a
+// job list that the next pass takes up, packed densely into warps.  The
+// lane's state between windows is its job record.
+constexpr uint32_t kWalkThreads = 64;
+constexpr uint32_t kWindowUnits = 128;
+constexpr uint32_t kWindowTile = (kWindowUnits + 4) * 4;     // bytes per lane
+constexpr uint32_t kWindowStride = kWindowTile;   // 132 words: 8 bank groups, 16-byte aligned
+
+struct WJob {          // stored as two uint4
+    uint32_t k;       // region whose merge walk this is
+    uint32_t b;       // block the cursors stand at (its start)
+    uint32_t a_rec;   // Gamma_k's entry at block b: rel | idx << 8
+    uint32_t ca;      // Gamma_k's count from region k's start
+    uint32_t g_rec;   // Gamma_{k+1}'s entry (replay cursor), ~0 = not started
+    uint32_t cg;      // Gamma_{k+1}'s count from region k + 1's start
+    uint32_t pad0, pad1;
+};
+static_assert(sizeof(WJob) == 32, "job record layout");
+
+__device__ __forceinline__ uint32_t walk_jobs(const DecodeParams& p, uint32_t pass) {
+    if (pass == 0) return p.nreg > 0 ? p.nreg - 1 : 0;
+    const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
+    return *(volatile uint32_t*) (p.scan_flags + ntile + 1 + ((pass - 1) & 1));
+}
+
+// One pass over job indices [jbase, jbase + blockDim.x).  Pass 0 takes
+// every region k < nreg - 1 implicitly; pass q > 0 reads list (q - 1) & 1.
+// Unfinished walks go to list q & 1 unless this is the last pass.
+__device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase, uint32_t pass,
+                                           uint32_t max_windows) {
+    extern __shared__ __align__(16) uint2 s_tab[];
+    const uint32_t njobs = walk_jobs(p, pass);
+    if (jbase >= njobs) return;   // whole CTA idle: skip the table load
+    load_prepared(s_tab, p.tab_sync, p.L);
+    if (*(volatile uint32_t*) p.status & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE)) return;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (jbase + (warp << 5) >= njobs) return;   // whole warp idle
+    const uint32_t tb = smem_addr(s_tab);
+    const uint32_t tab_bytes = (p.L * 8 + 15) & ~15u;
+    const uint32_t tile = tb + tab_bytes + threadIdx.x * kWindowStride;
+    const uint32_t bar = tb + tab_bytes + blockDim.x * kWindowStride + warp * 8;
+    const uint32_t* __restrict__ in = p.units;
+    const uint32_t n = p.n_units;
+    const uint32_t B = p.B, Bbits = p.B * 32, nwb = kWindowUnits / p.B;
+    const uint32_t tile_units = kWindowUnits + 4;
+    const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
+    WJob* lists = p.walk_jobs;
+
+    if (lane == 0) {
+        mbar_init(bar, 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+
+    const uint32_t j = jbase + threadIdx.x;
+    bool open = j < njobs;
+    uint32_t jk = 0, jb = 0, a_rec = 0, ca = 0, g_rec = ~0u, cg = 0;
+    if (open) {
+        if (pass == 0) {
+            jk = j;
+            jb = (j + 1) * p.nb;
+            const uint2 r0 = p.rec_w[(size_t) jb * p.dmax];
+            a_rec = r0.x;
+            ca = r0.y;
+        } else {
+            const uint4* src = reinterpret_cast<const uint4*>(
+                lists + (size_t) ((pass - 1) & 1) * p.nreg + j);
+            const uint4 v0 = src[0], v1 = src[1];
+            jk = v0.x; jb = v0.y; a_rec = v0.z; ca = v0.w; g_rec = v1.x; cg = v1.y;
+        }
+    }
+    bool timed_out = false;
+    bool first_block = pass == 0;   // the walk's first record exists already
+    for (uint32_t win = 0; __any_sync(0xffffffffu, open); ++win) {
+        if (win == max_windows) {
+            if (open) {
+                const uint32_t slot = atomicAdd(p.scan_flags + ntile + 1 + (pass & 1), 1u);
+                uint4* dst = reinterpret_cast<uint4*>(lists + (size_t) (pass & 1) * p.nreg + slot);
+                dst[0] = make_uint4(jk, jb, a_rec, ca);
+                dst[1] = make_uint4(g_rec, cg, 0u, 0u);
+            }
+            break;
+        }
+        // stage units [b * B, b * B + kWindowUnits + 4) of every open lane
+        const uint32_t u0 = jb * B;
+        const uint32_t avail = (open && u0 < n) ? min(tile_units, n - u0) : 0u;
+        const uint32_t bulk = avail & ~3u;
+        const uint32_t total = __reduce_add_sync(0xffffffffu, bulk * 4);
+        if (lane == 0) mbar_arrive_expect_tx(bar, total);
+        __syncwarp();
+        if (bulk) {
+            fence_proxy_async();
+            tma_load(tile, in + u0, bulk * 4, bar);
+        }
+        if (open)
+            for (uint32_t i = bulk; i < tile_units; ++i)
+                sts32(tile + i * 4, i < avail ? __ldg(in + u0 + i) : 0u);
+        if (!mbar_wait(bar, win & 1)) {
+            timed_out = true;
+            mbar_wait(bar, win & 1);
+        }
+        __syncwarp();
+        if (!open) continue;
+
+        const UnitSrc src{tile, u0, ~0u, tile_units - 1};
+        const uint64_t origin = (uint64_t) u0 * 32;
+        SCursor A, G;
+        A.init(src, origin, origin + (a_rec & 0xffu), tb + 8u * min(a_rec >> 8, p.L - 1));
+        const bool replay = g_rec != ~0u;
+        if (replay)
+            G.init(src, origin, origin + (g_rec & 0xffu), tb + 8u * min(g_rec >> 8, p.L - 1));
+        bool g_on = replay;
+        uint32_t bs = 0;
+        for (uint32_t i = 0; i < nwb && open; ++i) {
+            const uint32_t b = jb;
+            const uint32_t d = b / p.nb - jk;
+            if (d > p.dmax) {
+                atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
+                p.m[jk] = ~0ull;
+                p.delta[jk] = 0;
+                open = false;
+                break;
+            }
+            const uint32_t ax = (A.pos - bs) | (entry_index(A.a, tb) << 8);
+            if (!first_block) p.rec_w[(size_t) b * p.dmax + (d - 1)] = make_uint2(ax, ca);
+            first_block = false;
+            // Gamma_{k+1} at block b
+            uint32_t gx, gc;
+            if (d == 1) {
+                const uint2 rg = p.rec_g[b];
+                gx = rg.x;
+                gc = rg.y;
+            } else {
+                if (!g_on) {
+                    // entering region k + 2: Gamma_{k+1}'s entry from its G pass
+                    const uint2 r1 = p.rec_w[(size_t) b * p.dmax];
+                    G.init(src, origin, origin + bs + (r1.x & 0xffu),
+                           tb + 8u * min(r1.x >> 8, p.L - 1));
+                    cg = r1.y;
+                    g_on = true;
+                }
+                gx = (G.pos - bs) | (entry_index(G.a, tb) << 8);
+                gc = cg;
+            }
+            if (ax == gx) {
+                p.m[jk] = (uint64_t) b * Bbits + (ax & 0xffu);
+                p.delta[jk] = (long long) ca - (long long) gc;
+                open = false;
+                break;
+            }
+            // walk block b
+            const uint32_t be = bs + Bbits;
+            while (A.pos < be) ca += A.step(src) >> 24;
+            if (g_on)
+                while (G.pos < be) cg += G.step(src) >> 24;
+            bs = be;
+            jb = b + 1;
+            if (jb >= p.nblk) {
+                p.m[jk] = ~0ull;   // no merge before the stream end
+                p.delta[jk] = 0;
+                open = false;
+            }
+        }
+        if (open) {
+            a_rec = (A.pos - bs) | (entry_index(A.a, tb) << 8);
+            g_rec = g_on ? ((G.pos - bs) | (entry_index(G.a, tb) << 8)) : ~0u;
+        }
+    }
+    if (timed_out) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
+}
+
+__global__ void __launch_bounds__(kWalkThreads) k_wwalk(DecodeParams p, uint32_t pass,
+                                                        uint32_t max_windows) {
+    wwalk_body(p, blockIdx.x * blockDim.x, pass, max_windows);
 }
 
 // Exclusive prefix max of m (identity 0) and prefix sum of delta over the
@@ -341,9 +499,6 @@ __global__ void __launch_bounds__(kSyncThreads) k_sync(DecodeParams p) {
 // taken in launch order through an atomic ticket, so a tile only ever waits
 // on tiles that are already running or done; each wait is bounded and a
 // timeout sets MANS_DEV_SCAN_TIMEOUT instead of spinning on.
-constexpr uint32_t kScanThreads = 256;
-constexpr uint32_t kScanPer = 8;
-constexpr uint32_t kScanTile = kScanThreads * kScanPer;
 
 struct ScanTile {               // one per tile, 32 bytes
     unsigned long long agg_m;   // tile max
@@ -468,7 +623,7 @@ __device__ __forceinline__ bool block_entry(const DecodeParams& p, uint32_t b,
     }
     const uint2 rec = d == 0 ? p.rec_g[b] : p.rec_w[(size_t) b * p.dmax + (d - 1)];
     off = (unsigned long long) (p.Dpre[r - d] + (long long) rec.y);
-    idx = min(rec.x >> 8, p.L - 1);   // records come from k_sync; the clamp keeps
+    idx = min(rec.x >> 8, p.L - 1);   // records come from the sync stage; the clamp keeps
     rel = rec.x & 0xffu;              // table addresses in range regardless
     return true;
 }
@@ -653,12 +808,21 @@ __global__ void k_prep_batch(const DecodeParams* ps) {
     prep_body(sp);
 }
 
-__global__ void __launch_bounds__(kSyncThreads) k_sync_batch(const DecodeParams* ps,
-                                                             const BatchItem* items) {
+__global__ void __launch_bounds__(kSyncThreads) k_gwalk_batch(const DecodeParams* ps,
+                                                              const BatchItem* items) {
     __shared__ DecodeParams sp;
     const BatchItem it = items[blockIdx.x];
     load_params(sp, ps + it.stream);
-    sync_body(sp, it.index);
+    gwalk_body(sp, it.index);
+}
+
+__global__ void __launch_bounds__(kWalkThreads) k_wwalk_batch(const DecodeParams* ps,
+                                                              const BatchItem* items,
+                                                              uint32_t pass, uint32_t max_windows) {
+    __shared__ DecodeParams sp;
+    const BatchItem it = items[blockIdx.x];
+    load_params(sp, ps + it.stream);
+    wwalk_body(sp, it.index, pass, max_windows);
 }
 
 // The batch ticket hands out items in list order; the list holds each
@@ -689,10 +853,19 @@ __global__ void __launch_bounds__(kFinalThreads) k_final_batch(const DecodeParam
 
 struct AuxLayout {
     size_t rec_g, rec_w, m, delta, Mpre, Dpre, status, tab_sync, tab_sym, scan_tiles,
-        scan_flags, total;
+        scan_flags, walk_jobs, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
+
+// Merge-walk passes: windows per pass (the last pass runs walks to the end).
+constexpr uint32_t kWalkPasses = 3;
+constexpr uint32_t kWalkWindows[kWalkPasses] = {1, 3, 0xffffffffu};
+
+static size_t walk_smem(uint32_t L) {
+    return (((size_t) L * 8 + 15) & ~(size_t) 15) + (size_t) kWalkThreads * kWindowStride +
+           (kWalkThreads / 32) * 8;
+}
 
 // Opts the kernels in to large dynamic shared memory, once per device.
 static void set_kernel_attributes() {
@@ -703,10 +876,12 @@ static void set_kernel_attributes() {
     std::lock_guard<std::mutex> lock(mu);
     if (dev < 64 && ((done >> dev) & 1)) return;
     cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_sync, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_gwalk, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_wwalk, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_prep_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_sync_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_gwalk_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_wwalk_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_final_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (dev < 64) done |= 1ull << dev;
 }
@@ -725,7 +900,8 @@ static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax) {
     a.Dpre = o; o += align256(nreg * 8);
     const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
     a.scan_tiles = o; o += align256(ntiles * sizeof(ScanTile));
-    a.scan_flags = o; o += align256((ntiles + 1) * 4);   // flags, then the ticket
+    a.scan_flags = o; o += align256((ntiles + 3) * 4);   // flags, ticket, 2 list counts
+    a.walk_jobs = o; o += align256(2 * nreg * sizeof(WJob));
     a.total = o;
     return a;
 }
@@ -740,7 +916,7 @@ static thread_local uint32_t g_last_launches = 0;
 
 // Optional per-kernel timing: events recorded around each kernel of every
 // decode into a ring of slots, summed by mans_timing_collect.
-constexpr int kTimedKernels = 4;   // prep, sync, scan, final
+constexpr int kTimedKernels = 5;   // prep, gwalk, wwalk (3 passes), scan, final
 struct TimingState {
     bool on = false;
     int cap = 0, used = 0;
@@ -880,6 +1056,7 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     p.tab_sym = (uint2*) (base + lay.tab_sym);
     p.scan_tiles = (ScanTile*) (base + lay.scan_tiles);
     p.scan_flags = (uint32_t*) (base + lay.scan_flags);
+    p.walk_jobs = (WJob*) (base + lay.walk_jobs);
     p.n_out = n_out;
     p.n_units = (uint32_t) n_units;
     p.L = L;
@@ -893,7 +1070,7 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
 
     const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
     if (cudaMemsetAsync(p.status, 0, sizeof(uint32_t), st) != cudaSuccess ||
-        cudaMemsetAsync(base + lay.scan_flags, 0, (ntiles + 1) * 4, st) != cudaSuccess)
+        cudaMemsetAsync(base + lay.scan_flags, 0, (ntiles + 3) * 4, st) != cudaSuccess)
         return MANS_ERR_CUDA;
     const size_t smem = ((size_t) L * sizeof(uint2) + 15) & ~(size_t) 15;
     set_kernel_attributes();
@@ -903,6 +1080,7 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
     p.stage_cap = (uint32_t) ((cap + 15) & ~(uint64_t) 15);
     const size_t smem_sync = smem + (size_t) kSyncThreads * kRingStride + (kSyncThreads / 32) * 40;
+    const size_t smem_walk = walk_smem(L);
     const uint32_t tile_bytes = (cfg.block_units + 4) * 4;
     const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
     const size_t per_warp_final = (size_t) 32 * tile_stride + 16 + p.stage_cap + 16;
@@ -910,14 +1088,22 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     timing_mark(0, st);
     k_prep<<<1, 1024, (size_t) L * 12, st>>>(p);
     timing_mark(1, st);
-    k_sync<<<(unsigned) ((nreg + kSyncThreads - 1) / kSyncThreads), kSyncThreads, smem_sync, st>>>(p);
+    k_gwalk<<<(unsigned) ((nreg + kSyncThreads - 1) / kSyncThreads), kSyncThreads, smem_sync, st>>>(p);
     timing_mark(2, st);
-    k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(p);
+    uint32_t launches = 4;
+    if (nreg > 1) {
+        const unsigned ww = (unsigned) ((nreg - 1 + kWalkThreads - 1) / kWalkThreads);
+        for (uint32_t pass = 0; pass < kWalkPasses; ++pass)
+            k_wwalk<<<ww, kWalkThreads, smem_walk, st>>>(p, pass, kWalkWindows[pass]);
+        launches += kWalkPasses;
+    }
     timing_mark(3, st);
-    k_final<<<(unsigned) ((nblk + kFinalThreads - 1) / kFinalThreads), kFinalThreads, smem_final, st>>>(p);
+    k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(p);
     timing_mark(4, st);
+    k_final<<<(unsigned) ((nblk + kFinalThreads - 1) / kFinalThreads), kFinalThreads, smem_final, st>>>(p);
+    timing_mark(5, st);
     if (g_timing.on && g_timing.used < g_timing.cap) ++g_timing.used;
-    g_last_launches = 4;
+    g_last_launches = launches;
     if (cudaGetLastError() != cudaSuccess) return MANS_ERR_CUDA;
     return MANS_OK;
 }
@@ -1025,8 +1211,8 @@ struct BatchStreamPlan {
 
 struct BatchLayout {
     size_t status, flags, ticket, params, items, data, total;
-    size_t n_sync, n_scan, n_final, n_items;
-    size_t smem_sync, smem_final, smem_prep;
+    size_t n_sync, n_walk, n_scan, n_final, n_items;
+    size_t smem_sync, smem_walk, smem_final, smem_prep;
 };
 
 static size_t stream_data_bytes(const BatchStreamPlan& sp) {
@@ -1044,8 +1230,8 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
                       std::vector<BatchStreamPlan>& plans, BatchLayout& lay) {
     plans.assign(n, BatchStreamPlan{});
     size_t data = 0, flag_words = 0;
-    lay.n_sync = lay.n_scan = lay.n_final = 0;
-    lay.smem_sync = lay.smem_final = lay.smem_prep = 0;
+    lay.n_sync = lay.n_walk = lay.n_scan = lay.n_final = 0;
+    lay.smem_sync = lay.smem_walk = lay.smem_final = lay.smem_prep = 0;
     for (uint32_t i = 0; i < n; ++i) {
         BatchStreamPlan& sp = plans[i];
         sp.active = d[i].n_out > 0;
@@ -1063,10 +1249,12 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
         sp.data_off = data;
         data += align256(stream_data_bytes(sp));
         sp.flags_off = flag_words;
-        flag_words += sp.ntiles + 1;
+        flag_words += sp.ntiles + 3;
         sp.stage_cap = stage_cap_for((double) d[i].n_out / (double) d[i].n_units,
                                      sp.cfg.block_units);
         lay.n_sync += (sp.nreg + kSyncThreads - 1) / kSyncThreads;
+        if (sp.nreg > 1) lay.n_walk += (sp.nreg - 1 + kWalkThreads - 1) / kWalkThreads;
+        lay.smem_walk = std::max(lay.smem_walk, walk_smem(d[i].L));
         lay.n_scan += sp.ntiles;
         lay.n_final += (sp.nblk + kFinalThreads - 1) / kFinalThreads;
         const size_t tab = ((size_t) d[i].L * 8 + 15) & ~(size_t) 15;
@@ -1079,7 +1267,7 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
                                             ((size_t) 32 * tile_stride + 16 + sp.stage_cap + 16));
         lay.smem_prep = std::max(lay.smem_prep, (size_t) d[i].L * 12);
     }
-    lay.n_items = lay.n_sync + lay.n_scan + lay.n_final;
+    lay.n_items = lay.n_sync + lay.n_walk + lay.n_scan + lay.n_final;
     size_t o = 0;
     lay.status = o; o += align256((size_t) n * 4);
     lay.flags = o; o += align256(flag_words * 4);
@@ -1174,7 +1362,7 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
     b->slice.assign(n, nullptr);
     b->ps.assign(n, DecodeParams{});
     b->items.assign(b->lay.n_items, BatchItem{});
-    size_t is = 0, ic = b->lay.n_sync, iff = b->lay.n_sync + b->lay.n_scan;
+    size_t is = 0, iw = b->lay.n_sync, ic = iw + b->lay.n_walk, iff = ic + b->lay.n_scan;
     for (uint32_t i = 0; i < n; ++i) {
         const BatchStreamPlan& sp = b->plans[i];
         DecodeParams& p = b->ps[i];
@@ -1199,6 +1387,7 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         p.Dpre = (long long*) (slice + a.Dpre);
         p.scan_tiles = (ScanTile*) (slice + a.scan_tiles);
         p.scan_flags = (uint32_t*) (b->base + b->lay.flags) + sp.flags_off;
+        p.walk_jobs = (WJob*) (slice + a.walk_jobs);
         p.n_out = d.n_out;
         p.n_units = (uint32_t) d.n_units;
         p.L = d.L;
@@ -1211,6 +1400,7 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         p.nreg = (uint32_t) sp.nreg;
         p.stage_cap = sp.stage_cap;
         for (size_t r = 0; r < sp.nreg; r += kSyncThreads) b->items[is++] = {i, (uint32_t) r, 0, 0};
+        for (size_t r = 0; r + 1 < sp.nreg; r += kWalkThreads) b->items[iw++] = {i, (uint32_t) r, 0, 0};
         for (size_t t = 0; t < sp.ntiles; ++t) b->items[ic++] = {i, (uint32_t) t, 0, 0};
         const uint32_t nctas = (uint32_t) ((sp.nblk + kFinalThreads - 1) / kFinalThreads);
         for (uint32_t c = 0; c < nctas; ++c) b->items[iff++] = {i, c, nctas, 0};
@@ -1265,14 +1455,19 @@ int mans_batch_decode(mans_batch* b, void* stream) {
     const BatchItem* items = (const BatchItem*) (b->base + L.items);
     k_prep_batch<<<b->n, 1024, L.smem_prep, st>>>(ps);
     if (L.n_sync)
-        k_sync_batch<<<(unsigned) L.n_sync, kSyncThreads, L.smem_sync, st>>>(ps, items);
+        k_gwalk_batch<<<(unsigned) L.n_sync, kSyncThreads, L.smem_sync, st>>>(ps, items);
+    if (L.n_walk)
+        for (uint32_t pass = 0; pass < kWalkPasses; ++pass)
+            k_wwalk_batch<<<(unsigned) L.n_walk, kWalkThreads, L.smem_walk, st>>>(
+                ps, items + L.n_sync, pass, kWalkWindows[pass]);
     if (L.n_scan)
         k_scan_batch<<<(unsigned) L.n_scan, kScanThreads, 0, st>>>(
-            ps, items + L.n_sync, (uint32_t*) (b->base + L.ticket));
+            ps, items + L.n_sync + L.n_walk, (uint32_t*) (b->base + L.ticket));
     if (L.n_final)
         k_final_batch<<<(unsigned) L.n_final, kFinalThreads, L.smem_final, st>>>(
-            ps, items + L.n_sync + L.n_scan);
-    g_last_launches = 4;
+            ps, items + L.n_sync + L.n_walk + L.n_scan);
+    g_last_launches = 1 + (L.n_sync ? 1 : 0) + (L.n_walk ? kWalkPasses : 0) + (L.n_scan ? 1 : 0) +
+                      (L.n_final ? 1 : 0);
     return cudaGetLastError() == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
 }
 
@@ -1300,7 +1495,6 @@ int mans_batch_graph_decode(mans_batch* b, void* stream) {
         }
         b->graph = g;
     }
-    g_last_launches = 4;
     return cudaGraphLaunch(b->exec, (cudaStream_t) stream) == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
 }
 

@@ -342,7 +342,7 @@ struct mans_server {
         s->busy = true;
         std::lock_guard<std::mutex> lk(cq_mu);
         ++st.batches;
-        st.kernel_launches += 4;
+        st.kernel_launches += mans_last_launch_count();
         st.largest_batch = std::max<uint64_t>(st.largest_batch, n);
         return true;
     }
