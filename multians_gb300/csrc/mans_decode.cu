@@ -161,6 +161,19 @@ constexpr uint32_t kScanThreads = 256;
 constexpr uint32_t kScanPer = 8;
 constexpr uint32_t kScanTile = kScanThreads * kScanPer;
 
+// A merge walk not finished where it started, in the job lists of the
+// merge-walk passes (see k_wwalk).
+struct WJob {          // stored as two uint4
+    uint32_t k;       // region whose merge walk this is
+    uint32_t b;       // block the cursors stand at (its start)
+    uint32_t a_rec;   // Gamma_k's entry at block b: rel | idx << 8
+    uint32_t ca;      // Gamma_k's count from region k's start
+    uint32_t g_rec;   // Gamma_{k+1}'s entry (replay cursor), ~0 = not started
+    uint32_t cg;      // Gamma_{k+1}'s count from region k + 1's start
+    uint32_t pad0, pad1;
+};
+static_assert(sizeof(WJob) == 32, "job record layout");
+
 // Sync stage, G pass (k_gwalk): every lane owns a ring of kRingSlots chunks
 // of kChunk units in shared memory, filled by TMA bulk copies.  The warp
 // works in rounds; in one round every lane advances its cursor to the next
@@ -194,8 +207,15 @@ __device__ __forceinline__ void ring_fill(uint32_t slot_addr, const uint32_t* __
 
 // One lane per region k: decode Gamma_k over the region's blocks, record
 // every block's entry (rec_g) and, for k + 1 < nreg, Gamma_k's entry at the
-// first block of region k + 1 (walk slot 0 of that block), where the merge
-// walk of k_wwalk starts.  Every lane does the same amount of work.
+// first block of region k + 1 (walk slot 0 of that block).  Then the lane
+// starts region k's merge walk in the same ring: region k + 1 belongs to
+// the next lane, whose block records were written rounds earlier, so at
+// every block start of region k + 1 the lane compares Gamma_k with
+// Gamma_{k+1}'s record (read from L2, one block ahead).  A walk that has not
+// merged after kWalkCapUnits units, and the walk of the warp's last lane
+// (whose successor region belongs to another warp), go to the job list of
+// the merge-walk passes (k_wwalk).
+constexpr uint32_t kWalkCapUnits = 128;
 __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase) {
     extern __shared__ __align__(16) uint2 s_tab[];
     load_prepared(s_tab, p.tab_sync, p.L);
@@ -219,6 +239,7 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
     __syncwarp();
 
     bool active = k < p.nreg;
+    bool walking = false;   // merge walk (after the region's own blocks)
     const uint32_t b0 = min(k * p.nb, p.nblk);
     const uint32_t b1 = min(b0 + p.nb, p.nblk);
     const uint64_t origin = (uint64_t) b0 * Bbits;
@@ -251,14 +272,18 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
     uint32_t ca = 0;
     uint32_t b = b0;        // block being decoded
     uint32_t bs = 0;        // relative start bit of block b
+    uint32_t wend = 0;      // merge walk: last block start it may compare at
+    uint2 rg = make_uint2(0, 0);   // Gamma_{k+1}'s record at block b
     if (active) {
         A.init(rs, origin, start, tb + 8u * p.first_idx);
         p.rec_g[b0] = make_rec(A.pos, entry_index(A.a, tb), 0);
         if (b0 == b1) active = false;
     }
 
+    const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
     uint32_t r = 0;
     while (__any_sync(0xffffffffu, active)) {
+        __syncwarp();   // orders the records of earlier rounds for the other lanes
         // refill: wait for round r-2's copies, then issue this round's
         if (r >= 2 && !mbar_wait(bars + 8 * ((r - 2) & 3), ((r - 2) >> 2) & 1)) {
             timed_out = true;
@@ -275,7 +300,36 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
         if (lane == 0) mbar_arrive_expect_tx(bars + 8 * (r & 3), total);
         ++r;
 
-        if (active) {
+        if (active && walking) {
+            // merge walk at the start of block b (inside region k + 1)
+            const uint32_t ax = (A.pos - bs) | (entry_index(A.a, tb) << 8);
+            if (ax == rg.x) {
+                p.m[k] = (uint64_t) b * Bbits + (ax & 0xffu);
+                p.delta[k] = (long long) ca - (long long) rg.y;
+                active = false;
+            } else if (b == wend) {
+                const uint32_t slot = atomicAdd(p.scan_flags + ntile + 1, 1u);
+                uint4* dst = reinterpret_cast<uint4*>(p.walk_jobs + slot);
+                dst[0] = make_uint4(k, b, ax, ca);
+                dst[1] = make_uint4(~0u, 0u, 0u, 0u);
+                active = false;
+            } else {
+                // the next block's record was written rounds ago
+                const uint2 rg_next = b + 1 < p.nblk ? __ldcg(p.rec_g + b + 1) : make_uint2(0, 0);
+                const uint32_t be = bs + Bbits;
+                while (A.pos < be) ca += A.step(rs) >> 24;
+                ++b;
+                bs = be;
+                if (b >= p.nblk) {
+                    p.m[k] = ~0ull;   // no merge before the stream end
+                    p.delta[k] = 0;
+                    active = false;
+                } else {
+                    p.rec_w[(size_t) b * p.dmax] = make_rec(A.pos - bs, entry_index(A.a, tb), ca);
+                    rg = rg_next;
+                }
+            }
+        } else if (active) {
             // decode to the end of block b, record block b+1's entry
             const uint32_t be = bs + Bbits;
             while (A.pos < be) ca += A.step(rs) >> 24;
@@ -284,14 +338,24 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
             const uint2 rec = make_rec(A.pos - bs, entry_index(A.a, tb), ca);
             if (b < b1) {
                 p.rec_g[b] = rec;
-            } else {
-                if (k + 1 < p.nreg) {
-                    p.rec_w[(size_t) b1 * p.dmax] = rec;
-                } else {
-                    p.m[k] = ~0ull;   // the last region has no successor
-                    p.delta[k] = 0;
-                }
+            } else if (k + 1 >= p.nreg) {
+                p.m[k] = ~0ull;   // the last region has no successor
+                p.delta[k] = 0;
                 active = false;
+            } else {
+                p.rec_w[(size_t) b1 * p.dmax] = rec;
+                if (lane < 31) {
+                    // the successor region is the next lane's: walk on here
+                    walking = true;
+                    wend = b1 + min(kWalkCapUnits / p.B, p.nb - 1);
+                    rg = __ldcg(p.rec_g + b1);
+                } else {
+                    const uint32_t slot = atomicAdd(p.scan_flags + ntile + 1, 1u);
+                    uint4* dst = reinterpret_cast<uint4*>(p.walk_jobs + slot);
+                    dst[0] = make_uint4(k, b1, rec.x, rec.y);
+                    dst[1] = make_uint4(~0u, 0u, 0u, 0u);
+                    active = false;
+                }
             }
         }
     }
@@ -326,26 +390,15 @@ constexpr uint32_t kWindowUnits = 128;
 constexpr uint32_t kWindowTile = (kWindowUnits + 4) * 4;     // bytes per lane
 constexpr uint32_t kWindowStride = kWindowTile;   // 132 words: 8 bank groups, 16-byte aligned
 
-struct WJob {          // stored as two uint4
-    uint32_t k;       // region whose merge walk this is
-    uint32_t b;       // block the cursors stand at (its start)
-    uint32_t a_rec;   // Gamma_k's entry at block b: rel | idx << 8
-    uint32_t ca;      // Gamma_k's count from region k's start
-    uint32_t g_rec;   // Gamma_{k+1}'s entry (replay cursor), ~0 = not started
-    uint32_t cg;      // Gamma_{k+1}'s count from region k + 1's start
-    uint32_t pad0, pad1;
-};
-static_assert(sizeof(WJob) == 32, "job record layout");
 
 __device__ __forceinline__ uint32_t walk_jobs(const DecodeParams& p, uint32_t pass) {
-    if (pass == 0) return p.nreg > 0 ? p.nreg - 1 : 0;
     const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
     return *(volatile uint32_t*) (p.scan_flags + ntile + 1 + ((pass - 1) & 1));
 }
 
-// One pass over job indices [jbase, jbase + blockDim.x).  Pass 0 takes
-// every region k < nreg - 1 implicitly; pass q > 0 reads list (q - 1) & 1.
-// Unfinished walks go to list q & 1 unless this is the last pass.
+// One pass (1 or 2) over job indices [jbase, jbase + blockDim.x) of list
+// (pass - 1) & 1.  Unfinished walks go to list pass & 1 unless this is the
+// last pass (no window limit).
 __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase, uint32_t pass,
                                            uint32_t max_windows) {
     extern __shared__ __align__(16) uint2 s_tab[];
@@ -376,21 +429,12 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
     bool open = j < njobs;
     uint32_t jk = 0, jb = 0, a_rec = 0, ca = 0, g_rec = ~0u, cg = 0;
     if (open) {
-        if (pass == 0) {
-            jk = j;
-            jb = (j + 1) * p.nb;
-            const uint2 r0 = p.rec_w[(size_t) jb * p.dmax];
-            a_rec = r0.x;
-            ca = r0.y;
-        } else {
-            const uint4* src = reinterpret_cast<const uint4*>(
-                lists + (size_t) ((pass - 1) & 1) * p.nreg + j);
-            const uint4 v0 = src[0], v1 = src[1];
-            jk = v0.x; jb = v0.y; a_rec = v0.z; ca = v0.w; g_rec = v1.x; cg = v1.y;
-        }
+        const uint4* src = reinterpret_cast<const uint4*>(
+            lists + (size_t) ((pass - 1) & 1) * p.nreg + j);
+        const uint4 v0 = src[0], v1 = src[1];
+        jk = v0.x; jb = v0.y; a_rec = v0.z; ca = v0.w; g_rec = v1.x; cg = v1.y;
     }
     bool timed_out = false;
-    bool first_block = pass == 0;   // the walk's first record exists already
     for (uint32_t win = 0; __any_sync(0xffffffffu, open); ++win) {
         if (win == max_windows) {
             if (open) {
@@ -442,8 +486,7 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
                 break;
             }
             const uint32_t ax = (A.pos - bs) | (entry_index(A.a, tb) << 8);
-            if (!first_block) p.rec_w[(size_t) b * p.dmax + (d - 1)] = make_uint2(ax, ca);
-            first_block = false;
+            p.rec_w[(size_t) b * p.dmax + (d - 1)] = make_uint2(ax, ca);
             // Gamma_{k+1} at block b
             uint32_t gx, gc;
             if (d == 1) {
@@ -741,14 +784,26 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
         const uint32_t cnt = off < end ? (uint32_t) min(end - off, cap_sym) : 0u;
         const uint32_t pos_cap = p.B * 32 + kMaxBits + 1;
         const uint32_t full = off_nx >= off ? (uint32_t) min(off_nx - off, 0xffffffffull) : 0u;
-        SCursor c;
+        SCursorLazy c;
         const UnitSrc ts{tile, u0, ~0u, tile_units - 1};
         const uint64_t bs = (uint64_t) b * p.B * 32;   // cursor units are global indices
         c.init(ts, bs, bs + rel, tb + 8u * idx);
         if (staged) {
-            const uint32_t dst = stage_addr + phase + (uint32_t) (off - off0);
-            for (uint32_t i = 0; i < cnt && c.pos < pos_cap; ++i)
-                sts8(dst + i, c.step(ts) >> 24);
+            // bytes up to a word boundary, then four symbols per 32-bit
+            // store, then the remaining bytes
+            uint32_t q = stage_addr + phase + (uint32_t) (off - off0);
+            uint32_t i = 0;
+            for (; i < cnt && (q & 3u) && c.pos < pos_cap; ++i, ++q)
+                sts8(q, c.step(ts) >> 24);
+            for (; i + 4 <= cnt && c.pos < pos_cap; i += 4, q += 4) {
+                const uint32_t y0 = c.step(ts), y1 = c.step(ts);
+                const uint32_t y2 = c.step(ts), y3 = c.step(ts);
+                const uint32_t lo2 = __byte_perm(y0, y1, 0x0073);   // sym0 | sym1 << 8
+                const uint32_t hi2 = __byte_perm(y2, y3, 0x7300);   // sym2 << 16 | sym3 << 24
+                sts32(q, __byte_perm(lo2, hi2, 0x7610));
+            }
+            for (; i < cnt && c.pos < pos_cap; ++i, ++q)
+                sts8(q, c.step(ts) >> 24);
         } else {
             uint8_t* dst = p.out + off;
             for (uint32_t i = 0; i < cnt && c.pos < pos_cap; ++i)
@@ -859,8 +914,8 @@ struct AuxLayout {
 static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
 
 // Merge-walk passes: windows per pass (the last pass runs walks to the end).
-constexpr uint32_t kWalkPasses = 3;
-constexpr uint32_t kWalkWindows[kWalkPasses] = {1, 3, 0xffffffffu};
+constexpr uint32_t kWalkPasses = 2;   // passes 1 and 2 (the G pass opens the walks)
+constexpr uint32_t kWalkWindows[kWalkPasses] = {3, 0xffffffffu};
 
 static size_t walk_smem(uint32_t L) {
     return (((size_t) L * 8 + 15) & ~(size_t) 15) + (size_t) kWalkThreads * kWindowStride +
@@ -1093,8 +1148,8 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     uint32_t launches = 4;
     if (nreg > 1) {
         const unsigned ww = (unsigned) ((nreg - 1 + kWalkThreads - 1) / kWalkThreads);
-        for (uint32_t pass = 0; pass < kWalkPasses; ++pass)
-            k_wwalk<<<ww, kWalkThreads, smem_walk, st>>>(p, pass, kWalkWindows[pass]);
+        for (uint32_t pass = 1; pass <= kWalkPasses; ++pass)
+            k_wwalk<<<ww, kWalkThreads, smem_walk, st>>>(p, pass, kWalkWindows[pass - 1]);
         launches += kWalkPasses;
     }
     timing_mark(3, st);
@@ -1457,9 +1512,9 @@ int mans_batch_decode(mans_batch* b, void* stream) {
     if (L.n_sync)
         k_gwalk_batch<<<(unsigned) L.n_sync, kSyncThreads, L.smem_sync, st>>>(ps, items);
     if (L.n_walk)
-        for (uint32_t pass = 0; pass < kWalkPasses; ++pass)
+        for (uint32_t pass = 1; pass <= kWalkPasses; ++pass)
             k_wwalk_batch<<<(unsigned) L.n_walk, kWalkThreads, L.smem_walk, st>>>(
-                ps, items + L.n_sync, pass, kWalkWindows[pass]);
+                ps, items + L.n_sync, pass, kWalkWindows[pass - 1]);
     if (L.n_scan)
         k_scan_batch<<<(unsigned) L.n_scan, kScanThreads, 0, st>>>(
             ps, items + L.n_sync + L.n_walk, (uint32_t*) (b->base + L.ticket));

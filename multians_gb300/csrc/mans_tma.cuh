@@ -87,17 +87,29 @@ struct UnitSrc {
 // branches on this step's result, so the dependent chain per symbol is one
 // shared load plus two integer operations.  The window lo:hi holds the
 // bits [pos, top); a refill is due when fewer than 32 remain
-// (pos > lim = top - 32).  Every step loads the unit a refill would take,
-// together with the table entry and before either is needed: a load issued
-// only on the lanes that refill would leave the warp waiting on another
-// lane's load into the same register on most steps.
-struct SCursor {
+// (pos > lim = top - 32).
+//
+// Where the unit a refill takes comes from is a trade between latency and
+// shared-memory bandwidth:
+//  * kLazy = false: every step loads it, next to the table entry and before
+//    either is needed.  A load issued only on the refilling lanes would make
+//    the whole warp wait for it at the next refill of any lane (one
+//    register, one scoreboard).  Best where the per-symbol chain latency
+//    bounds the kernel (the sync walks).
+//  * kLazy = true: it is already in a register (nu); a refill consumes it
+//    and loads the following unit.  A step takes at most kMaxBits bits, so
+//    refills are at least two steps apart and only refilling lanes touch
+//    shared memory for units: about a fifth of the unit wavefronts.  Best
+//    where shared-memory wavefronts bound the kernel (the final pass).
+template <bool kLazy>
+struct SCursorT {
     uint2 e;         // table entry of the current state
     uint32_t a;      // shared address of that entry
     uint32_t lo, hi; // bit window
     uint32_t pos;    // bit position of the next codeword (relative)
     uint32_t lim;    // refill when pos > lim
-    uint32_t next;   // global index of the next unit to load
+    uint32_t next;   // global index of the next unit a refill takes
+    uint32_t nu;     // that unit (kLazy only)
 
     __device__ __forceinline__ void init(const UnitSrc& src, uint64_t origin, uint64_t abs,
                                          uint32_t entry_addr) {
@@ -110,11 +122,12 @@ struct SCursor {
         hi = w1 >> o;
         lim = pos - o + 32;     // top = pos - o + 64
         next = u + 2;
+        if (kLazy) nu = src(next);
     }
 
     // One step; returns y (mask | k << 16 | count-or-symbol << 24).
     __device__ __forceinline__ uint32_t step(const UnitSrc& src) {
-        const uint32_t u = src(next);
+        const uint32_t u = kLazy ? nu : src(next);
         const uint32_t y = e.y;
         const uint32_t b = lo & y & 0xffffu;
         a = e.x + (b << 3);
@@ -129,9 +142,13 @@ struct SCursor {
             hi = u >> (32 - avail);
             lim += 32;
             ++next;
+            if (kLazy) nu = src(next);
         }
         return y;
     }
 };
+
+using SCursor = SCursorT<false>;
+using SCursorLazy = SCursorT<true>;
 
 }  // namespace mans
