@@ -177,17 +177,21 @@ static_assert(sizeof(WJob) == 32, "job record layout");
 // Sync stage, G pass (k_gwalk): every lane owns a ring of kRingSlots chunks
 // of kChunk units in shared memory, filled by TMA bulk copies.  The warp
 // works in rounds; in one round every lane advances its cursor to the next
-// block start (at most kMaxBlockUnits units plus a step).  Between rounds
-// each lane releases its oldest chunk w once its cursor has loaded past
-// unit 32(w+1) + kRelease and refills that slot with chunk w + 4.  Reads
-// stay inside chunks w and w + 1, so a chunk copied in round r is first
-// read in round r + 2 and round r waits only for the copies of round r - 2.
-constexpr uint32_t kChunk = 32;                    // units per ring slot
+// half-block boundary, so its unit loads advance at most
+// kMaxBlockUnits / 2 + 3 = 11 units.  At the start of a round each lane
+// releases its oldest chunk w once its cursor has loaded past unit
+// 16(w+1) + kRelease and refills that slot with chunk w + 4; the cursor is
+// then less than 11 units past that threshold, so rounds r and r + 1 read
+// below unit 16(w+1) + 36 < 16(w+4), the start of the new chunk: a chunk
+// copied in round r is first read in round r + 2, and round r waits only
+// for the copies of round r - 2.  The small ring (272 bytes a lane) keeps
+// 20 warps of walks resident per SM.
+constexpr uint32_t kChunk = 16;                    // units per ring slot
 constexpr uint32_t kRingSlots = 4;
 constexpr uint32_t kRingUnits = kChunk * kRingSlots;
-constexpr uint32_t kRingStride = kRingUnits * 4 + 16;   // bytes per lane (padded)
+constexpr uint32_t kRingStride = kRingUnits * 4 + 16;   // bytes per lane: 68 words, 8 bank groups
 constexpr uint32_t kRelease = 4;
-constexpr uint32_t kSyncThreads = 64;
+constexpr uint32_t kSyncThreads = 128;
 constexpr uint32_t kMaxBlockUnits = 16;
 constexpr uint32_t kMaxWalkSlots = 12;
 
@@ -228,7 +232,7 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
     const uint32_t k = rbase + threadIdx.x;
     const uint32_t* __restrict__ in = p.units;
     const uint32_t n = p.n_units;
-    const uint32_t Bbits = p.B * 32;
+    const uint32_t Bbits = p.B * 32, Hbits = p.B * 16;
     const UnitSrc rs{ring, 0u, kRingUnits - 1, kRingUnits - 1};
 
     if ((rbase + (warp << 5)) >= p.nreg) return;   // whole warp idle
@@ -271,9 +275,11 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
     SCursor A;
     uint32_t ca = 0;
     uint32_t b = b0;        // block being decoded
-    uint32_t bs = 0;        // relative start bit of block b
+    uint32_t bs = 0;        // relative start bit of the current half block
+    uint32_t half = 0;      // 0: first half of block b, 1: second half
     uint32_t wend = 0;      // merge walk: last block start it may compare at
-    uint2 rg = make_uint2(0, 0);   // Gamma_{k+1}'s record at block b
+    uint2 rg = make_uint2(0, 0);       // Gamma_{k+1}'s record at block b
+    uint2 rg_next = make_uint2(0, 0);  // ... at block b + 1 (loaded ahead)
     if (active) {
         A.init(rs, origin, start, tb + 8u * p.first_idx);
         p.rec_g[b0] = make_rec(A.pos, entry_index(A.a, tb), 0);
@@ -300,7 +306,7 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
         if (lane == 0) mbar_arrive_expect_tx(bars + 8 * (r & 3), total);
         ++r;
 
-        if (active && walking) {
+        if (active && walking && half == 0) {
             // merge walk at the start of block b (inside region k + 1)
             const uint32_t ax = (A.pos - bs) | (entry_index(A.a, tb) << 8);
             if (ax == rg.x) {
@@ -313,48 +319,49 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
                 dst[0] = make_uint4(k, b, ax, ca);
                 dst[1] = make_uint4(~0u, 0u, 0u, 0u);
                 active = false;
-            } else {
-                // the next block's record was written rounds ago
-                const uint2 rg_next = b + 1 < p.nblk ? __ldcg(p.rec_g + b + 1) : make_uint2(0, 0);
-                const uint32_t be = bs + Bbits;
-                while (A.pos < be) ca += A.step(rs) >> 24;
+            } else if (b + 1 < p.nblk) {
+                rg_next = __ldcg(p.rec_g + b + 1);   // written rounds ago
+            }
+        }
+        if (active) {
+            // decode to the end of the half block
+            const uint32_t be = bs + Hbits;
+            while (A.pos < be) ca += A.step(rs) >> 24;
+            bs = be;
+            half ^= 1u;
+            if (half == 0) {
+                // block b done: record block b+1's entry
                 ++b;
-                bs = be;
-                if (b >= p.nblk) {
-                    p.m[k] = ~0ull;   // no merge before the stream end
+                const uint2 rec = make_rec(A.pos - bs, entry_index(A.a, tb), ca);
+                if (walking) {
+                    if (b >= p.nblk) {
+                        p.m[k] = ~0ull;   // no merge before the stream end
+                        p.delta[k] = 0;
+                        active = false;
+                    } else {
+                        p.rec_w[(size_t) b * p.dmax] = rec;
+                        rg = rg_next;
+                    }
+                } else if (b < b1) {
+                    p.rec_g[b] = rec;
+                } else if (k + 1 >= p.nreg) {
+                    p.m[k] = ~0ull;   // the last region has no successor
                     p.delta[k] = 0;
                     active = false;
                 } else {
-                    p.rec_w[(size_t) b * p.dmax] = make_rec(A.pos - bs, entry_index(A.a, tb), ca);
-                    rg = rg_next;
-                }
-            }
-        } else if (active) {
-            // decode to the end of block b, record block b+1's entry
-            const uint32_t be = bs + Bbits;
-            while (A.pos < be) ca += A.step(rs) >> 24;
-            ++b;
-            bs = be;
-            const uint2 rec = make_rec(A.pos - bs, entry_index(A.a, tb), ca);
-            if (b < b1) {
-                p.rec_g[b] = rec;
-            } else if (k + 1 >= p.nreg) {
-                p.m[k] = ~0ull;   // the last region has no successor
-                p.delta[k] = 0;
-                active = false;
-            } else {
-                p.rec_w[(size_t) b1 * p.dmax] = rec;
-                if (lane < 31) {
-                    // the successor region is the next lane's: walk on here
-                    walking = true;
-                    wend = b1 + min(kWalkCapUnits / p.B, p.nb - 1);
-                    rg = __ldcg(p.rec_g + b1);
-                } else {
-                    const uint32_t slot = atomicAdd(p.scan_flags + ntile + 1, 1u);
-                    uint4* dst = reinterpret_cast<uint4*>(p.walk_jobs + slot);
-                    dst[0] = make_uint4(k, b1, rec.x, rec.y);
-                    dst[1] = make_uint4(~0u, 0u, 0u, 0u);
-                    active = false;
+                    p.rec_w[(size_t) b1 * p.dmax] = rec;
+                    if (lane < 31) {
+                        // the successor region is the next lane's: walk on here
+                        walking = true;
+                        wend = b1 + min(kWalkCapUnits / p.B, p.nb - 1);
+                        rg = __ldcg(p.rec_g + b1);
+                    } else {
+                        const uint32_t slot = atomicAdd(p.scan_flags + ntile + 1, 1u);
+                        uint4* dst = reinterpret_cast<uint4*>(p.walk_jobs + slot);
+                        dst[0] = make_uint4(k, b1, rec.x, rec.y);
+                        dst[1] = make_uint4(~0u, 0u, 0u, 0u);
+                        active = false;
+                    }
                 }
             }
         }
