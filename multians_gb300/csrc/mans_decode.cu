@@ -921,8 +921,11 @@ struct AuxLayout {
 static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
 
 // Merge-walk passes: windows per pass (the last pass runs walks to the end).
-constexpr uint32_t kWalkPasses = 2;   // passes 1 and 2 (the G pass opens the walks)
-constexpr uint32_t kWalkWindows[kWalkPasses] = {3, 0xffffffffu};
+// One pass without a window limit: the walks still open after the G pass
+// include the stream's longest, and starting them at once keeps that chain
+// off the critical path of a second pass.
+constexpr uint32_t kWalkPasses = 1;   // pass 1 (the G pass opens the walks)
+constexpr uint32_t kWalkWindows[kWalkPasses] = {0xffffffffu};
 
 static size_t walk_smem(uint32_t L) {
     return (((size_t) L * 8 + 15) & ~(size_t) 15) + (size_t) kWalkThreads * kWindowStride +
