@@ -167,10 +167,12 @@ struct WJob {          // stored as two uint4
     uint32_t k;       // region whose merge walk this is
     uint32_t b;       // block the cursors stand at (its start)
     uint32_t a_rec;   // Gamma_k's entry at block b: rel | idx << 8
-    uint32_t ca;      // Gamma_k's count from region k's start
+    uint32_t ca;      // Gamma_k's count from region k's start (while A
+                      // follows the region's trajectory: the offset to it)
     uint32_t g_rec;   // Gamma_{k+1}'s entry (replay cursor), ~0 = not started
-    uint32_t cg;      // Gamma_{k+1}'s count from region k + 1's start
-    uint32_t pad0, pad1;
+    uint32_t cg;      // Gamma_{k+1}'s count from region k + 1's start (or offset)
+    uint32_t flags;   // 1: A follows, 2: G follows the current region's trajectory
+    uint32_t pad;
 };
 static_assert(sizeof(WJob) == 32, "job record layout");
 
@@ -403,9 +405,18 @@ __device__ __forceinline__ uint32_t walk_jobs(const DecodeParams& p, uint32_t pa
     return *(volatile uint32_t*) (p.scan_flags + ntile + 1 + ((pass - 1) & 1));
 }
 
-// One pass (1 or 2) over job indices [jbase, jbase + blockDim.x) of list
-// (pass - 1) & 1.  Unfinished walks go to list pass & 1 unless this is the
-// last pass (no window limit).
+// One pass over job indices [jbase, jbase + blockDim.x) of list
+// (pass - 1) & 1.  Unfinished walks go to list pass & 1 after max_windows
+// windows (0xffffffff: no limit).
+//
+// Past region k + 1 both trajectories are cursors (A = Gamma_k, G =
+// Gamma_{k+1}), stepped interleaved.  A cursor that meets the current
+// region's own trajectory Gamma_j at a block start stops being stepped: it
+// equals Gamma_j from there on, so its entry at every later block of region
+// j is rec_g's and its count is rec_g's plus a fixed offset; at the next
+// region start it resumes from Gamma_j's entry there (walk slot 0, from the
+// G pass).  Once both cursors follow Gamma_j their entries coincide, which
+// is the merge.
 __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase, uint32_t pass,
                                            uint32_t max_windows) {
     extern __shared__ __align__(16) uint2 s_tab[];
@@ -425,6 +436,7 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
     const uint32_t tile_units = kWindowUnits + 4;
     const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
     WJob* lists = p.walk_jobs;
+    constexpr uint32_t kAFollow = 1u, kGFollow = 2u;
 
     if (lane == 0) {
         mbar_init(bar, 1);
@@ -434,12 +446,14 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
 
     const uint32_t j = jbase + threadIdx.x;
     bool open = j < njobs;
-    uint32_t jk = 0, jb = 0, a_rec = 0, ca = 0, g_rec = ~0u, cg = 0;
+    // job: region jk, block jb; A: entry a_rec, count ca (offset to Gamma_j's
+    // count while following); G likewise (g_rec = ~0: not a cursor yet)
+    uint32_t jk = 0, jb = 0, a_rec = 0, ca = 0, g_rec = ~0u, cg = 0, fl = 0;
     if (open) {
         const uint4* src = reinterpret_cast<const uint4*>(
             lists + (size_t) ((pass - 1) & 1) * p.nreg + j);
         const uint4 v0 = src[0], v1 = src[1];
-        jk = v0.x; jb = v0.y; a_rec = v0.z; ca = v0.w; g_rec = v1.x; cg = v1.y;
+        jk = v0.x; jb = v0.y; a_rec = v0.z; ca = v0.w; g_rec = v1.x; cg = v1.y; fl = v1.z;
     }
     bool timed_out = false;
     for (uint32_t win = 0; __any_sync(0xffffffffu, open); ++win) {
@@ -448,11 +462,11 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
                 const uint32_t slot = atomicAdd(p.scan_flags + ntile + 1 + (pass & 1), 1u);
                 uint4* dst = reinterpret_cast<uint4*>(lists + (size_t) (pass & 1) * p.nreg + slot);
                 dst[0] = make_uint4(jk, jb, a_rec, ca);
-                dst[1] = make_uint4(g_rec, cg, 0u, 0u);
+                dst[1] = make_uint4(g_rec, cg, fl, 0u);
             }
             break;
         }
-        // stage units [b * B, b * B + kWindowUnits + 4) of every open lane
+        // stage units [jb * B, jb * B + kWindowUnits + 4) of every open lane
         const uint32_t u0 = jb * B;
         const uint32_t avail = (open && u0 < n) ? min(tile_units, n - u0) : 0u;
         const uint32_t bulk = avail & ~3u;
@@ -466,6 +480,8 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
         if (open)
             for (uint32_t i = bulk; i < tile_units; ++i)
                 sts32(tile + i * 4, i < avail ? __ldg(in + u0 + i) : 0u);
+        // Gamma_j's record at the window's first block, while the copy lands
+        uint2 rg = (open && jb < p.nblk) ? __ldcg(p.rec_g + jb) : make_uint2(0, 0);
         if (!mbar_wait(bar, win & 1)) {
             timed_out = true;
             mbar_wait(bar, win & 1);
@@ -476,15 +492,16 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
         const UnitSrc src{tile, u0, ~0u, tile_units - 1};
         const uint64_t origin = (uint64_t) u0 * 32;
         SCursor A, G;
-        A.init(src, origin, origin + (a_rec & 0xffu), tb + 8u * min(a_rec >> 8, p.L - 1));
-        const bool replay = g_rec != ~0u;
-        if (replay)
+        if (!(fl & kAFollow))
+            A.init(src, origin, origin + (a_rec & 0xffu), tb + 8u * min(a_rec >> 8, p.L - 1));
+        if (g_rec != ~0u && !(fl & kGFollow))
             G.init(src, origin, origin + (g_rec & 0xffu), tb + 8u * min(g_rec >> 8, p.L - 1));
-        bool g_on = replay;
+        uint32_t reg = jb / p.nb;                 // region of block jb
+        uint32_t reg_end = (reg + 1) * p.nb;      // first block of the next region
         uint32_t bs = 0;
         for (uint32_t i = 0; i < nwb && open; ++i) {
             const uint32_t b = jb;
-            const uint32_t d = b / p.nb - jk;
+            const uint32_t d = reg - jk;
             if (d > p.dmax) {
                 atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
                 p.m[jk] = ~0ull;
@@ -492,39 +509,62 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
                 open = false;
                 break;
             }
-            const uint32_t ax = (A.pos - bs) | (entry_index(A.a, tb) << 8);
-            p.rec_w[(size_t) b * p.dmax + (d - 1)] = make_uint2(ax, ca);
-            // Gamma_{k+1} at block b
-            uint32_t gx, gc;
-            if (d == 1) {
-                const uint2 rg = p.rec_g[b];
-                gx = rg.x;
-                gc = rg.y;
-            } else {
-                if (!g_on) {
-                    // entering region k + 2: Gamma_{k+1}'s entry from its G pass
-                    const uint2 r1 = p.rec_w[(size_t) b * p.dmax];
-                    G.init(src, origin, origin + bs + (r1.x & 0xffu),
-                           tb + 8u * min(r1.x >> 8, p.L - 1));
-                    cg = r1.y;
-                    g_on = true;
+            if (d >= 2 && b == reg * p.nb) {
+                // region start: a following cursor resumes from Gamma_{j-1}'s
+                // entry here; G starts here as Gamma_{k+1}'s entry
+                const uint2 r1 = p.rec_w[(size_t) b * p.dmax];
+                if (fl & kAFollow) {
+                    A.init(src, origin, origin + bs + (r1.x & 0xffu), tb + 8u * min(r1.x >> 8, p.L - 1));
+                    ca += r1.y;
+                    fl &= ~kAFollow;
                 }
-                gx = (G.pos - bs) | (entry_index(G.a, tb) << 8);
-                gc = cg;
+                if (g_rec == ~0u || (fl & kGFollow)) {
+                    G.init(src, origin, origin + bs + (r1.x & 0xffu), tb + 8u * min(r1.x >> 8, p.L - 1));
+                    cg = g_rec == ~0u ? r1.y : cg + r1.y;
+                    g_rec = 0;   // G is a cursor from here on
+                    fl &= ~kGFollow;
+                }
             }
+            // entries and counts of both trajectories at block b
+            const bool af = fl & kAFollow, gf = fl & kGFollow;
+            const uint32_t ax = af ? rg.x : (A.pos - bs) | (entry_index(A.a, tb) << 8);
+            const uint32_t cab = af ? rg.y + ca : ca;
+            uint32_t gx, cgb;
+            if (d == 1) {
+                gx = rg.x;
+                cgb = rg.y;
+            } else {
+                gx = gf ? rg.x : (G.pos - bs) | (entry_index(G.a, tb) << 8);
+                cgb = gf ? rg.y + cg : cg;
+            }
+            p.rec_w[(size_t) b * p.dmax + (d - 1)] = make_uint2(ax, cab);
             if (ax == gx) {
                 p.m[jk] = (uint64_t) b * Bbits + (ax & 0xffu);
-                p.delta[jk] = (long long) ca - (long long) gc;
+                p.delta[jk] = (long long) cab - (long long) cgb;
                 open = false;
                 break;
             }
-            // walk block b
+            if (d >= 2) {
+                // a cursor meeting Gamma_j follows it from here
+                if (!af && ax == rg.x) { fl |= kAFollow; ca -= rg.y; }
+                if (!gf && gx == rg.x) { fl |= kGFollow; cg -= rg.y; }
+            }
+            const uint2 rg_next = b + 1 < p.nblk ? __ldcg(p.rec_g + b + 1) : make_uint2(0, 0);
+            // walk block b with the cursors that do not follow
             const uint32_t be = bs + Bbits;
-            while (A.pos < be) ca += A.step(src) >> 24;
-            if (g_on)
-                while (G.pos < be) cg += G.step(src) >> 24;
+            const bool sa = !(fl & kAFollow), sg = d >= 2 && !(fl & kGFollow);
+            if (sa && sg) {
+                while (A.pos < be && G.pos < be) {
+                    ca += A.step(src) >> 24;
+                    cg += G.step(src) >> 24;
+                }
+            }
+            if (sa) while (A.pos < be) ca += A.step(src) >> 24;
+            if (sg) while (G.pos < be) cg += G.step(src) >> 24;
             bs = be;
             jb = b + 1;
+            rg = rg_next;
+            if (jb == reg_end) { ++reg; reg_end += p.nb; }
             if (jb >= p.nblk) {
                 p.m[jk] = ~0ull;   // no merge before the stream end
                 p.delta[jk] = 0;
@@ -532,8 +572,8 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
             }
         }
         if (open) {
-            a_rec = (A.pos - bs) | (entry_index(A.a, tb) << 8);
-            g_rec = g_on ? ((G.pos - bs) | (entry_index(G.a, tb) << 8)) : ~0u;
+            if (!(fl & kAFollow)) a_rec = (A.pos - bs) | (entry_index(A.a, tb) << 8);
+            if (g_rec != ~0u && !(fl & kGFollow)) g_rec = (G.pos - bs) | (entry_index(G.a, tb) << 8);
         }
     }
     if (timed_out) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);

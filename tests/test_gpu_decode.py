@@ -68,6 +68,21 @@ def test_geometries(mg, oracle_lib, cfg):
     assert np.array_equal(got[::-1], st.symbols)
 
 
+@pytest.mark.parametrize("L,lam,cfg", [
+    (4096, 0.05, {"block_units": 8, "region_blocks": 9, "walk_slots": 12}),
+    (4096, 0.5, {"block_units": 4, "region_blocks": 9, "walk_slots": 12}),
+    (1024, 0.005, {"block_units": 16, "region_blocks": 9, "walk_slots": 6}),
+    (1024, 2.0, {"block_units": 4, "region_blocks": 9, "walk_slots": 12}),
+])
+def test_walks_across_regions(mg, oracle_lib, L, lam, cfg):
+    """Sync distances of several regions: merge walks run on with two
+    cursors, which follow the trajectories of the regions they cross."""
+    O = oracle_lib
+    st = O.make_stream(seed=4242 + L, lam=lam, n=300_000, L=L)
+    got = _gpu_decode(mg, st, cfg=cfg)
+    assert np.array_equal(got[::-1], st.symbols)
+
+
 def test_async_geometry_clean(mg, oracle_lib):
     """Long regions with spare slots: one asynchronous pass, status clean."""
     O = oracle_lib
