@@ -274,7 +274,7 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
         __syncwarp();
     }
 
-    SCursor A;
+    SCursorLazy A;   // 17+ warps per SM: shared-memory wavefronts bound this pass
     uint32_t ca = 0;
     uint32_t b = b0;        // block being decoded
     uint32_t bs = 0;        // relative start bit of the current half block

@@ -58,64 +58,6 @@ __device__ __forceinline__ void load_prepared(uint2* s_tab, const uint2* __restr
     __syncthreads();
 }
 
-// Stream bit reader for one decoder, LSB first.  A 64-bit window lo:hi
-// holds 32..63 valid bits; the next unit is prefetched into `pre` one
-// refill ahead so the global load latency stays off the decode chain.  The
-// prefetch reads a clamped (always in-bounds) address and keeps the
-// "past the end" test apart, applying it only when the unit is used: a
-// select right after the load would make every refill wait for memory.
-// Positions are bit offsets relative to `origin` (a 64-bit bit address).
-// Units at index >= n read as zero.
-struct Cursor {
-    uint32_t a;      // shared address of the current state's entry
-    uint32_t lo, hi; // bit window
-    uint32_t avail;  // valid bits in the window
-    uint32_t pos;    // bit position of the next codeword (relative)
-    uint32_t next;   // global index of the unit in `pre`
-    uint32_t pre;    // prefetched unit (valid only if next < n)
-
-    __device__ __forceinline__ static uint32_t ld(const uint32_t* __restrict__ in,
-                                                  uint32_t n, uint32_t i) {
-        return i < n ? __ldg(in + i) : 0u;
-    }
-
-    // Places the cursor at absolute bit position `abs` (pos = abs - origin).
-    __device__ __forceinline__ void init(const uint32_t* __restrict__ in, uint32_t n,
-                                         uint64_t origin, uint64_t abs,
-                                         uint32_t entry_addr) {
-        a = entry_addr;
-        pos = (uint32_t) (abs - origin);
-        const uint32_t u = (uint32_t) (abs >> 5), o = (uint32_t) (abs & 31);
-        const uint32_t w0 = ld(in, n, u), w1 = ld(in, n, u + 1);
-        lo = __funnelshift_r(w0, w1, o);
-        hi = w1 >> o;
-        avail = 64 - o;
-        next = u + 2;
-        pre = __ldg(in + min(next, n - 1));
-    }
-
-    // One step; returns the entry's y word (mask / k / count or symbol).
-    __device__ __forceinline__ uint32_t step(const uint32_t* __restrict__ in, uint32_t n) {
-        const uint2 e = lds64(a);
-        const uint32_t b = lo & e.y & 0xffffu;
-        a = e.x + (b << 3);
-        const uint32_t k = __byte_perm(e.y, 0, 0x4442);
-        lo = __funnelshift_r(lo, hi, k);
-        hi >>= k;
-        avail -= k;
-        pos += k;
-        if (avail < 32) {
-            const uint32_t u = next < n ? pre : 0u;
-            lo |= u << avail;
-            hi = u >> (32 - avail);
-            avail += 32;
-            ++next;
-            pre = __ldg(in + min(next, n - 1));
-        }
-        return e.y;
-    }
-};
-
 __device__ __forceinline__ uint32_t entry_index(uint32_t a, uint32_t tab_base) {
     return (a - tab_base) >> 3;
 }

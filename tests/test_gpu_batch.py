@@ -33,7 +33,7 @@ def test_batch_uneven_streams_direct_and_graph(mg):
     for i in range(60):
         n = int(np.exp(rng.uniform(np.log(10), np.log(400_000))))
         lam = float(rng.uniform(0.01, 2.0))
-        L = 1024 if i % 3 else 4096
+        L = (1024, 4096, 8192)[i % 3]   # shared tables of 8, 32 and 64 KB in one batch
         specs.append((1000 + i, lam, n, L))
     specs += [(5, 0.05, 1, 1024), (6, 2.0, 2, 1024), (7, 0.3, 33, 4096)]
     streams = _streams(host, specs)

@@ -33,9 +33,10 @@ def _gpu_decode(mg, st, n_out=None, cfg=None, sync=True):
     return out[:n_out].cpu().numpy()
 
 
-@pytest.mark.parametrize("L", [1024, 4096])
+@pytest.mark.parametrize("L", [1024, 4096, 8192])
 @pytest.mark.parametrize("lam", LAMBDAS)
 def test_roundtrip_vs_oracle(mg, oracle_lib, L, lam):
+    """Up to L = 8192, the largest table the shared-memory decoder holds."""
     O = oracle_lib
     st = O.make_stream(seed=1000 + int(lam * 1000) + L, lam=lam, n=300_000, L=L)
     got = _gpu_decode(mg, st)
