@@ -265,8 +265,8 @@ int mans_host_encode(const uint8_t* sym, size_t n, uint32_t L, uint32_t table_se
  * device array inside this library (mans_noalloc_scratch_bytes), held by
  * every GPU that loads the library until exit.  Same arguments and result
  * as mans_decode_sync; streams whose planned workspace exceeds the array
- * (about 13 million units at 6 bits/symbol) get MANS_ERR_AUX_SMALL before
- * any GPU work.  All calls on a device share the array: calls that overlap
+ * (about 6.4 million units at 6 bits/symbol, 1.7 million at 0.67 bits/symbol)
+ * get MANS_ERR_AUX_SMALL before any GPU work.  All calls on a device share the array: calls that overlap
  * on the GPU race, so serialise them.  The first call on a device looks up
  * the array's address and should come before any stream capture.
  * Synchronous on `stream`. */

@@ -13,9 +13,9 @@
 //  * the array holds kScratchBytes (32 MiB) and every GPU that loads the
 //    library keeps it until the process exits;
 //  * a stream is accepted when the workspace of its planned geometry fits
-//    (about 13 million units, ~50 MB of compressed input, at the default
-//    geometry for 6 bits per symbol); larger streams get MANS_ERR_AUX_SMALL
-//    before any GPU work;
+//    (about 6.4 million units, ~26 MB of compressed input, at 6 bits per
+//    symbol; about 1.7 million units at 0.67 bits per symbol); larger
+//    streams get MANS_ERR_AUX_SMALL before any GPU work;
 //  * every call on a device shares the one array and it keeps the last
 //    call's contents: calls that overlap on the GPU (another stream, another
 //    host thread) race and must be serialised by the caller.  The decode

@@ -1,0 +1,53 @@
+// Drop-in check of the reference's C++ API against this library: builds
+// tables and a stream with ANSTableGenerator / ANSEncoder and decodes it
+// with cuhd::CUHDGPUDecoder::decode through the GPU buffer classes, in the
+// call sequence a reference user writes (reference demo,
+// src/main.cc:52-125), then compares with the source via CUHDUtil::equals.
+// Prints one line per case and exits nonzero on any mismatch.
+#include <cmath>
+#include <cstdio>
+#include <memory>
+
+#include "multians.h"
+
+static bool run_case(double lambda, size_t n, size_t states) {
+    const size_t seed = 5, symbols = 256;
+    auto dist = ANSTableGenerator::generate_distribution(
+        seed, symbols, states, [lambda](double x) { return lambda * std::exp(-lambda * x); });
+    auto data = ANSTableGenerator::generate_test_data(dist.dist, n, states, seed);
+    auto table = ANSTableGenerator::generate_table(dist.prob, dist.dist, nullptr, symbols, states);
+    auto enc = ANSTableGenerator::generate_encoder_table(table);
+    auto dec = ANSTableGenerator::get_decoder_table(enc);
+    auto in = ANSEncoder::encode(data->data(), n, enc);
+    auto out = std::make_shared<CUHDOutputBuffer>(n);
+
+    auto g_in = std::make_shared<cuhd::CUHDGPUInputBuffer>(in);
+    auto g_tab = std::make_shared<cuhd::CUHDGPUCodetable>(dec);
+    auto g_out = std::make_shared<cuhd::CUHDGPUOutputBuffer>(out);
+    auto g_mem = std::make_shared<cuhd::CUHDGPUDecoderMemory>(in->get_compressed_size(), 4, 128);
+    g_tab->allocate();
+    g_in->allocate();
+    g_out->allocate();
+    g_mem->allocate();
+    g_tab->cpy_host_to_device();
+    g_in->cpy_host_to_device();
+    cuhd::CUHDGPUDecoder::decode(g_in, in->get_compressed_size(), g_out,
+                                 out->get_uncompressed_size(), g_tab, g_mem,
+                                 in->get_first_state(), in->get_first_bit(),
+                                 dec->get_num_entries(), 11, 4, 128);
+    g_out->cpy_device_to_host();
+    out->reverse();
+    const bool ok = cuhd::CUHDUtil::equals(data->data(), out->get_decompressed_data().get(), n);
+    std::printf("lambda=%.2f L=%zu n=%zu units=%zu %s\n", lambda, states, n,
+                in->get_compressed_size(), ok ? "ok" : "MISMATCH");
+    return ok;
+}
+
+int main() {
+    bool ok = true;
+    ok &= run_case(0.10, 1 << 20, 1024);
+    ok &= run_case(0.90, 3 << 20, 1024);
+    ok &= run_case(2.00, 1 << 20, 4096);
+    ok &= run_case(0.02, 777777, 4096);
+    return ok ? 0 : 1;
+}
