@@ -84,30 +84,33 @@ struct UnitSrc {
 // Bit cursor over units held in shared memory, software-pipelined: the
 // table entry of the current state is already in registers (e), and each
 // step issues the shared load of the next entry before anything that
-// branches on this step's result, so the dependent chain per symbol is one
-// shared load plus two integer operations.  The window lo:hi holds the
-// bits [pos, top); a refill is due when fewer than 32 remain
-// (pos > lim = top - 32).
+// depends on this step's result, so the dependent chain per symbol is one
+// shared load plus two integer operations.  The window is two units w0:w1
+// (the units next - 2 and next - 1) and the next codeword starts at bit
+// o < 32 of it: a step extracts 32 bits at o (one funnel shift, computed
+// from the previous step's o before the entry arrives), moves o by k <= 16,
+// and when o reaches 32 shifts the window by one unit (selects, no
+// branch).
 //
 // Where the unit a refill takes comes from is a trade between latency and
 // shared-memory bandwidth:
 //  * kLazy = false: every step loads it, next to the table entry and before
 //    either is needed.  A load issued only on the refilling lanes would make
 //    the whole warp wait for it at the next refill of any lane (one
-//    register, one scoreboard).  Best where the per-symbol chain latency
-//    bounds the kernel (the sync walks).
+//    register, one scoreboard) unless enough other warps hide that wait.
+//    Used where few warps run (the merge-walk passes).
 //  * kLazy = true: it is already in a register (nu); a refill consumes it
 //    and loads the following unit.  A step takes at most kMaxBits bits, so
 //    refills are at least two steps apart and only refilling lanes touch
-//    shared memory for units: about a fifth of the unit wavefronts.  Best
-//    where shared-memory wavefronts bound the kernel (the final pass).
+//    shared memory for units: about a fifth of the unit wavefronts.  Used
+//    where many warps share an SM and wavefronts bound the kernel.
 template <bool kLazy>
 struct SCursorT {
     uint2 e;         // table entry of the current state
     uint32_t a;      // shared address of that entry
-    uint32_t lo, hi; // bit window
+    uint32_t w0, w1; // window: units next - 2 and next - 1
+    uint32_t o;      // bit offset of the next codeword in w0:w1 (< 32)
     uint32_t pos;    // bit position of the next codeword (relative)
-    uint32_t lim;    // refill when pos > lim
     uint32_t next;   // global index of the next unit a refill takes
     uint32_t nu;     // that unit (kLazy only)
 
@@ -116,11 +119,10 @@ struct SCursorT {
         a = entry_addr;
         e = lds64(a);
         pos = (uint32_t) (abs - origin);
-        const uint32_t u = (uint32_t) (abs >> 5), o = (uint32_t) (abs & 31);
-        const uint32_t w0 = src(u), w1 = src(u + 1);
-        lo = __funnelshift_r(w0, w1, o);
-        hi = w1 >> o;
-        lim = pos - o + 32;     // top = pos - o + 64
+        const uint32_t u = (uint32_t) (abs >> 5);
+        o = (uint32_t) (abs & 31);
+        w0 = src(u);
+        w1 = src(u + 1);
         next = u + 2;
         if (kLazy) nu = src(next);
     }
@@ -129,21 +131,18 @@ struct SCursorT {
     __device__ __forceinline__ uint32_t step(const UnitSrc& src) {
         const uint32_t u = kLazy ? nu : src(next);
         const uint32_t y = e.y;
-        const uint32_t b = lo & y & 0xffffu;
-        a = e.x + (b << 3);
+        const uint32_t bits = __funnelshift_r(w0, w1, o);
+        a = e.x + ((bits & y & 0xffffu) << 3);
         e = lds64(a);
         const uint32_t k = __byte_perm(y, 0, 0x4442);
-        lo = __funnelshift_r(lo, hi, k);
-        hi >>= k;
         pos += k;
-        if (pos > lim) {
-            const uint32_t avail = lim + 32 - pos;   // 16..31
-            lo |= u << avail;
-            hi = u >> (32 - avail);
-            lim += 32;
-            ++next;
-            if (kLazy) nu = src(next);
-        }
+        o += k;
+        const bool r = o >= 32;    // at most one unit per step: o < 32, k <= 16
+        w0 = r ? w1 : w0;
+        w1 = r ? u : w1;
+        o = r ? o - 32 : o;
+        next += r ? 1u : 0u;
+        if (kLazy && r) nu = src(next);
         return y;
     }
 };
