@@ -11,8 +11,9 @@
 //           and records for every block of the region the first codeword
 //           at or after the block start and Gamma_k's symbol count before
 //           it, and Gamma_k's entry at the first block of region k + 1.
-//  k_wwalk  (three passes) keeps walking Gamma_k past its region end,
-//           comparing it at every block start with Gamma_{k+1}, until the
+//  k_wwalk  keeps walking Gamma_k past its region end (the G pass starts
+//           each walk; this pass finishes the longer ones), comparing it
+//           at every block start with Gamma_{k+1}, until the
 //           two trajectories meet at the same bit position in the same
 //           state: the merge point m_k.  Gamma_k's count minus
 //           Gamma_{k+1}'s count at m_k is delta_k.  Blocks the walk crosses
@@ -38,6 +39,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -63,7 +65,7 @@ struct DecodeParams {
     long long* Dpre;            // [nreg] prefix sum of delta
     uint32_t* status;
     struct ScanTile* scan_tiles;   // [ntiles] look-back records
-    struct WJob* walk_jobs;        // [2][nreg] merge-walk job lists
+    struct WJob* walk_jobs;        // [nreg] merge-walk jobs
     uint32_t* scan_flags;          // [ntiles] look-back flags, then the tile ticket
     unsigned long long n_out;
     uint32_t n_units;
@@ -76,6 +78,7 @@ struct DecodeParams {
     uint32_t nblk;
     uint32_t nreg;
     uint32_t stage_cap;    // staging bytes per warp in k_final (multiple of 16)
+    uint32_t wcap;         // blocks a merge walk may run inside the G pass
 };
 
 // Checks and converts the reference table, then builds both shared-memory
@@ -161,8 +164,8 @@ constexpr uint32_t kScanThreads = 256;
 constexpr uint32_t kScanPer = 8;
 constexpr uint32_t kScanTile = kScanThreads * kScanPer;
 
-// A merge walk not finished where it started, in the job lists of the
-// merge-walk passes (see k_wwalk).
+// A merge walk the G pass did not finish, in the job list of the
+// merge-walk pass (see k_wwalk).
 struct WJob {          // stored as two uint4
     uint32_t k;       // region whose merge walk this is
     uint32_t b;       // block the cursors stand at (its start)
@@ -193,7 +196,8 @@ constexpr uint32_t kRingSlots = 4;
 constexpr uint32_t kRingUnits = kChunk * kRingSlots;
 constexpr uint32_t kRingStride = kRingUnits * 4 + 16;   // bytes per lane: 68 words, 8 bank groups
 constexpr uint32_t kRelease = 4;
-constexpr uint32_t kSyncThreads = 128;
+constexpr uint32_t kSyncThreads = 128;      // batch launches; plain launches use
+constexpr uint32_t kSyncThreadsMax = 256;   // 256 for L >= 4096 (one table per 8 warps)
 constexpr uint32_t kMaxBlockUnits = 16;
 constexpr uint32_t kMaxWalkSlots = 12;
 
@@ -220,7 +224,7 @@ __device__ __forceinline__ void ring_fill(uint32_t slot_addr, const uint32_t* __
 // Gamma_{k+1}'s record (read from L2, one block ahead).  A walk that has not
 // merged after kWalkCapUnits units, and the walk of the warp's last lane
 // (whose successor region belongs to another warp), go to the job list of
-// the merge-walk passes (k_wwalk).
+// the merge-walk pass (k_wwalk).
 constexpr uint32_t kWalkCapUnits = 128;
 __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase) {
     extern __shared__ __align__(16) uint2 s_tab[];
@@ -355,7 +359,7 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
                     if (lane < 31) {
                         // the successor region is the next lane's: walk on here
                         walking = true;
-                        wend = b1 + min(kWalkCapUnits / p.B, p.nb - 1);
+                        wend = b1 + p.wcap;
                         rg = __ldcg(p.rec_g + b1);
                     } else {
                         const uint32_t slot = atomicAdd(p.scan_flags + ntile + 1, 1u);
@@ -378,36 +382,25 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
     if (timed_out) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
 }
 
-__global__ void __launch_bounds__(kSyncThreads) k_gwalk(DecodeParams p) {
+__global__ void __launch_bounds__(kSyncThreadsMax) k_gwalk(DecodeParams p) {
     gwalk_body(p, blockIdx.x * blockDim.x);
 }
 
 // Sync stage, merge walks (k_wwalk): region k's walk continues Gamma_k from
-// the first block of region k + 1 and stops at the first block start where
-// it meets Gamma_{k+1}: inside region k + 1 Gamma_{k+1} is known from its
-// block records (rec_g), so one cursor suffices; past region k + 1 a second
+// where the G pass left it and stops at the first block start where it
+// meets Gamma_{k+1}: inside region k + 1 Gamma_{k+1} is known from its block
+// records (rec_g), so one cursor suffices; past region k + 1 a second
 // cursor replays Gamma_{k+1} from its entry at region k + 2 (walk slot 0 of
-// that block, written by region k + 1's G pass).  Walks are short on
-// average but their lengths vary a lot, so they run in passes: each lane
-// stages a window of kWindowUnits units (plus 4 of look-ahead) with one
-// TMA copy and walks at most that window per round; a pass allows
-// `max_windows` rounds, and walks still open after that are appended to a
-// job list that the next pass takes up, packed densely into warps.  The
-// lane's state between windows is its job record.
-constexpr uint32_t kWalkThreads = 64;
-constexpr uint32_t kWindowUnits = 128;
-constexpr uint32_t kWindowTile = (kWindowUnits + 4) * 4;     // bytes per lane
-constexpr uint32_t kWindowStride = kWindowTile;   // 132 words: 8 bank groups, 16-byte aligned
-
-
-__device__ __forceinline__ uint32_t walk_jobs(const DecodeParams& p, uint32_t pass) {
-    const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
-    return *(volatile uint32_t*) (p.scan_flags + ntile + 1 + ((pass - 1) & 1));
-}
-
-// One pass over job indices [jbase, jbase + blockDim.x) of list
-// (pass - 1) & 1.  Unfinished walks go to list pass & 1 after max_windows
-// windows (0xffffffff: no limit).
+// that block, written by region k + 1's G pass).
+//
+// The walks the G pass hands over (its job list) vary a lot in length, so
+// warps take them one lane at a time: a warp works in rounds; at the start
+// of a round every lane without a walk takes the next job (one atomic per
+// warp), then each lane stages a window of kWindowUnits units (plus 4 of
+// look-ahead) with one TMA copy and walks at most that window.  A lane's
+// state between windows is its job record.  The grid is persistent (at most
+// a few CTAs per SM); warps leave when the list is exhausted and their
+// lanes are done.
 //
 // Past region k + 1 both trajectories are cursors (A = Gamma_k, G =
 // Gamma_{k+1}), stepped interleaved.  A cursor that meets the current
@@ -417,15 +410,21 @@ __device__ __forceinline__ uint32_t walk_jobs(const DecodeParams& p, uint32_t pa
 // region start it resumes from Gamma_j's entry there (walk slot 0, from the
 // G pass).  Once both cursors follow Gamma_j their entries coincide, which
 // is the merge.
-__device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase, uint32_t pass,
-                                           uint32_t max_windows) {
+constexpr uint32_t kWalkThreads = 64;
+constexpr uint32_t kWalkCtasMax = 152 * 8;
+constexpr uint32_t kWindowUnits = 128;
+constexpr uint32_t kWindowTile = (kWindowUnits + 4) * 4;     // bytes per lane
+constexpr uint32_t kWindowStride = kWindowTile;   // 132 words: 8 bank groups, 16-byte aligned
+
+__device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
     extern __shared__ __align__(16) uint2 s_tab[];
-    const uint32_t njobs = walk_jobs(p, pass);
-    if (jbase >= njobs) return;   // whole CTA idle: skip the table load
+    const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
+    uint32_t* const job_next = p.scan_flags + ntile + 2;   // next job to take
+    const uint32_t njobs = *(volatile uint32_t*) (p.scan_flags + ntile + 1);
+    if (njobs == 0 || *(volatile uint32_t*) job_next >= njobs) return;   // nothing left
     load_prepared(s_tab, p.tab_sync, p.L);
     if (*(volatile uint32_t*) p.status & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE)) return;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (jbase + (warp << 5) >= njobs) return;   // whole warp idle
     const uint32_t tb = smem_addr(s_tab);
     const uint32_t tab_bytes = (p.L * 8 + 15) & ~15u;
     const uint32_t tile = tb + tab_bytes + threadIdx.x * kWindowStride;
@@ -434,8 +433,7 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
     const uint32_t n = p.n_units;
     const uint32_t B = p.B, Bbits = p.B * 32, nwb = kWindowUnits / p.B;
     const uint32_t tile_units = kWindowUnits + 4;
-    const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
-    WJob* lists = p.walk_jobs;
+    const WJob* lists = p.walk_jobs;
     constexpr uint32_t kAFollow = 1u, kGFollow = 2u;
 
     if (lane == 0) {
@@ -444,28 +442,31 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
     }
     __syncwarp();
 
-    const uint32_t j = jbase + threadIdx.x;
-    bool open = j < njobs;
+    bool open = false, exhausted = false;
     // job: region jk, block jb; A: entry a_rec, count ca (offset to Gamma_j's
     // count while following); G likewise (g_rec = ~0: not a cursor yet)
     uint32_t jk = 0, jb = 0, a_rec = 0, ca = 0, g_rec = ~0u, cg = 0, fl = 0;
-    if (open) {
-        const uint4* src = reinterpret_cast<const uint4*>(
-            lists + (size_t) ((pass - 1) & 1) * p.nreg + j);
-        const uint4 v0 = src[0], v1 = src[1];
-        jk = v0.x; jb = v0.y; a_rec = v0.z; ca = v0.w; g_rec = v1.x; cg = v1.y; fl = v1.z;
-    }
     bool timed_out = false;
-    for (uint32_t win = 0; __any_sync(0xffffffffu, open); ++win) {
-        if (win == max_windows) {
-            if (open) {
-                const uint32_t slot = atomicAdd(p.scan_flags + ntile + 1 + (pass & 1), 1u);
-                uint4* dst = reinterpret_cast<uint4*>(lists + (size_t) (pass & 1) * p.nreg + slot);
-                dst[0] = make_uint4(jk, jb, a_rec, ca);
-                dst[1] = make_uint4(g_rec, cg, fl, 0u);
+    for (uint32_t win = 0;; ++win) {
+        // lanes without a walk take the next jobs
+        const uint32_t need = __ballot_sync(0xffffffffu, !open);
+        if (need && !exhausted) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(job_next, __popc(need));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            exhausted = base + __popc(need) >= njobs;
+            if (!open) {
+                const uint32_t jj = base + __popc(need & ((1u << lane) - 1));
+                if (jj < njobs) {
+                    const uint4* src = reinterpret_cast<const uint4*>(lists + jj);
+                    const uint4 v0 = src[0], v1 = src[1];
+                    jk = v0.x; jb = v0.y; a_rec = v0.z; ca = v0.w;
+                    g_rec = v1.x; cg = v1.y; fl = v1.z;
+                    open = true;
+                }
             }
-            break;
         }
+        if (!__any_sync(0xffffffffu, open)) break;
         // stage units [jb * B, jb * B + kWindowUnits + 4) of every open lane
         const uint32_t u0 = jb * B;
         const uint32_t avail = (open && u0 < n) ? min(tile_units, n - u0) : 0u;
@@ -579,10 +580,7 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p, uint32_t jbase
     if (timed_out) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
 }
 
-__global__ void __launch_bounds__(kWalkThreads) k_wwalk(DecodeParams p, uint32_t pass,
-                                                        uint32_t max_windows) {
-    wwalk_body(p, blockIdx.x * blockDim.x, pass, max_windows);
-}
+__global__ void __launch_bounds__(kWalkThreads) k_wwalk(DecodeParams p) { wwalk_body(p); }
 
 // Exclusive prefix max of m (identity 0) and prefix sum of delta over the
 // regions: single-pass decoupled look-back.  Tiles of kScanTile regions are
@@ -729,7 +727,7 @@ __device__ __forceinline__ bool block_entry(const DecodeParams& p, uint32_t b,
 // 16-byte phase as the output, then the warp writes the range with 16-byte
 // stores (bytes at the unaligned ends).  A range larger than the staging
 // buffer is written byte by byte instead.
-constexpr uint32_t kFinalThreads = 128;
+constexpr uint32_t kFinalThreads = 256;   // eight warps share one table copy
 
 __device__ __forceinline__ void sts8(uint32_t a, uint32_t v) {
     asm volatile("st.shared.u8 [%0], %1;" :: "r"(a), "r"(v) : "memory");
@@ -919,12 +917,11 @@ __global__ void __launch_bounds__(kSyncThreads) k_gwalk_batch(const DecodeParams
 }
 
 __global__ void __launch_bounds__(kWalkThreads) k_wwalk_batch(const DecodeParams* ps,
-                                                              const BatchItem* items,
-                                                              uint32_t pass, uint32_t max_windows) {
+                                                              const BatchItem* items) {
     __shared__ DecodeParams sp;
     const BatchItem it = items[blockIdx.x];
     load_params(sp, ps + it.stream);
-    wwalk_body(sp, it.index, pass, max_windows);
+    wwalk_body(sp);
 }
 
 // The batch ticket hands out items in list order; the list holds each
@@ -960,12 +957,21 @@ struct AuxLayout {
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
 
-// Merge-walk passes: windows per pass (the last pass runs walks to the end).
-// One pass without a window limit: the walks still open after the G pass
-// include the stream's longest, and starting them at once keeps that chain
-// off the critical path of a second pass.
-constexpr uint32_t kWalkPasses = 1;   // pass 1 (the G pass opens the walks)
-constexpr uint32_t kWalkWindows[kWalkPasses] = {0xffffffffu};
+// CTAs of the merge-walk pass for a stream of nreg regions (persistent:
+// warps take jobs until the list is exhausted).
+static uint32_t walk_ctas(size_t nreg) {
+    if (nreg < 2) return 0;
+    return (uint32_t) std::min<size_t>((nreg - 1 + kWalkThreads - 1) / kWalkThreads, kWalkCtasMax);
+}
+
+// Blocks a merge walk may run inside the G pass before it goes to the
+// merge-walk pass: at most kWalkCapUnits units and half a region (the warp
+// waits for its longest walk, so the cap bounds that wait).
+static uint32_t walk_cap(const mans_cfg& c) {
+    const uint32_t cap = std::min<uint32_t>(kWalkCapUnits / c.block_units,
+                                            std::max<uint32_t>(2, c.region_blocks / 2));
+    return std::max<uint32_t>(1, std::min<uint32_t>(cap, c.region_blocks - 1));
+}
 
 static size_t walk_smem(uint32_t L) {
     return (((size_t) L * 8 + 15) & ~(size_t) 15) + (size_t) kWalkThreads * kWindowStride +
@@ -1005,8 +1011,8 @@ static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax) {
     a.Dpre = o; o += align256(nreg * 8);
     const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
     a.scan_tiles = o; o += align256(ntiles * sizeof(ScanTile));
-    a.scan_flags = o; o += align256((ntiles + 3) * 4);   // flags, ticket, 2 list counts
-    a.walk_jobs = o; o += align256(2 * nreg * sizeof(WJob));
+    a.scan_flags = o; o += align256((ntiles + 3) * 4);   // flags, ticket, job count, next job
+    a.walk_jobs = o; o += align256(nreg * sizeof(WJob));
     a.total = o;
     return a;
 }
@@ -1052,6 +1058,28 @@ const char* mans_version(void) { return "multians_gb300 0.1"; }
 
 uint32_t mans_last_launch_count(void) { return g_last_launches; }
 
+// Mean distance (units) after which a decode started from the guessed
+// state meets the true one, measured on the generator's data (CPU
+// simulation over 4 M symbols per point) at L = 1024 and L = 4096 for
+// 0.67 .. 8.6 bits per symbol; interpolated linearly in bits per symbol and
+// in log2(L), extrapolated in proportion to L outside that range.
+static double mean_meeting_units(uint32_t L, double bits_per_symbol) {
+    static const double kBps[6] = {0.67, 1.5, 2.5, 3.8, 6.0, 8.6};
+    static const double kD1024[6] = {65, 143, 175, 153, 75, 28};
+    static const double kD4096[6] = {278, 567, 700, 630, 324, 65};
+    const double x = std::min(std::max(bits_per_symbol, kBps[0]), kBps[5]);
+    int i = 0;
+    while (i < 4 && x > kBps[i + 1]) ++i;
+    const double t = (x - kBps[i]) / (kBps[i + 1] - kBps[i]);
+    const double d1 = kD1024[i] + t * (kD1024[i + 1] - kD1024[i]);
+    const double d4 = kD4096[i] + t * (kD4096[i + 1] - kD4096[i]);
+    const double lg = std::log2((double) std::max<uint32_t>(L, 2));
+    if (lg <= 10) return d1 * (double) L / 1024.0;
+    if (lg >= 12) return d4 * (double) L / 4096.0;
+    const double u = (lg - 10) / 2;
+    return d1 + u * (d4 - d1);
+}
+
 int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
               mans_cfg* out) {
     if (!out || n_units == 0 || L < 2 || L > kMaxStates) return MANS_ERR_ARG;
@@ -1066,19 +1094,27 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
     c.block_units = std::min<uint32_t>(std::max<uint32_t>(c.block_units & ~3u, 4), kMaxBlockUnits);
     // Sync walks: a walk runs from a region's end until its trajectory meets
     // the next region's guessed one, crossing up to walk_slots regions.  The
-    // meeting distance grows with L; measured on the generator's data its
-    // tail passes 1.5 L units about once per thousand regions, so regions and
-    // slots are sized for R * (slots - 1) >= 4 L.  A walk that still runs out
-    // is reported (MANS_DEV_SYNC_OVERFLOW) and redone with longer regions.
+    // meeting distance grows with L (on the generator's data its mean is
+    // about 0.08 L units and its tail passes 1.5 L units about once per
+    // thousand regions), so slots are sized for R * (slots - 1) >= 4 L.  A
+    // walk that still runs out is reported (MANS_DEV_SYNC_OVERFLOW) and
+    // redone with longer regions.
+    //
+    // Region length R: one lane decodes a region, so R sets the parallelism
+    // (about 78 k lanes, 16 warps on every SM, when the stream is long
+    // enough) against the walk work (a walk per region, of the mean meeting
+    // distance).  R is the length that gives that many regions, kept between
+    // three mean meeting distances and 512 units (2048 for L > 1024; more
+    // when three meeting distances are longer): measured over 0.67 .. 8.6
+    // bits per symbol and L = 1024 / 4096, between about 2.5 and 4 meeting
+    // distances is best.
     const uint64_t tail = std::max<uint64_t>(256, 4ull * L);
-    const uint64_t r_min = (tail + kMaxWalkSlots - 2) / (kMaxWalkSlots - 1);
     if (c.region_blocks == 0) {
-        uint64_t R = L <= 1024 ? 512 : 2048;  // units per sync region
-        // keep at least ~4 regions per SM when the stream is small
-        const uint64_t want_regions = 152ull * 4;
-        while (R > r_min && n_units / R < want_regions) R /= 2;
-        R = std::max<uint64_t>(R, std::min<uint64_t>(r_min, 8ull * c.block_units));
-        R = std::max<uint64_t>(R, r_min);
+        const uint64_t lanes = 152ull * 16 * 32;
+        const uint64_t r_sync = (uint64_t) (3.0 * mean_meeting_units(L, 32.0 / std::max(sym_per_unit, 1e-3)));
+        const uint64_t r_max = std::max<uint64_t>(L <= 1024 ? 512 : 2048, r_sync);
+        uint64_t R = (n_units + lanes - 1) / lanes;
+        R = std::min<uint64_t>(std::max<uint64_t>(R, std::max<uint64_t>(r_sync, 64)), r_max);
         // an odd block count keeps lanes of a warp (one region each) off
         // power-of-two strides, which would pile them into the same L1 sets
         c.region_blocks = (uint32_t) std::max<uint64_t>(8, R / c.block_units) | 1u;
@@ -1172,6 +1208,7 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     p.dmax = cfg.walk_slots;
     p.nblk = (uint32_t) nblk;
     p.nreg = (uint32_t) nreg;
+    p.wcap = walk_cap(cfg);
 
     const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
     if (cudaMemsetAsync(p.status, 0, sizeof(uint32_t), st) != cudaSuccess ||
@@ -1184,7 +1221,8 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     uint64_t cap = (uint64_t) (per_unit * 32.0 * cfg.block_units * 1.5) + 256;
     cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
     p.stage_cap = (uint32_t) ((cap + 15) & ~(uint64_t) 15);
-    const size_t smem_sync = smem + (size_t) kSyncThreads * kRingStride + (kSyncThreads / 32) * 40;
+    const uint32_t gthreads = L >= 4096 ? kSyncThreadsMax : kSyncThreads;
+    const size_t smem_sync = smem + (size_t) gthreads * kRingStride + (gthreads / 32) * 40;
     const size_t smem_walk = walk_smem(L);
     const uint32_t tile_bytes = (cfg.block_units + 4) * 4;
     const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
@@ -1193,14 +1231,12 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     timing_mark(0, st);
     k_prep<<<1, 1024, (size_t) L * 12, st>>>(p);
     timing_mark(1, st);
-    k_gwalk<<<(unsigned) ((nreg + kSyncThreads - 1) / kSyncThreads), kSyncThreads, smem_sync, st>>>(p);
+    k_gwalk<<<(unsigned) ((nreg + gthreads - 1) / gthreads), gthreads, smem_sync, st>>>(p);
     timing_mark(2, st);
     uint32_t launches = 4;
-    if (nreg > 1) {
-        const unsigned ww = (unsigned) ((nreg - 1 + kWalkThreads - 1) / kWalkThreads);
-        for (uint32_t pass = 1; pass <= kWalkPasses; ++pass)
-            k_wwalk<<<ww, kWalkThreads, smem_walk, st>>>(p, pass, kWalkWindows[pass - 1]);
-        launches += kWalkPasses;
+    if (const uint32_t ww = walk_ctas(nreg)) {
+        k_wwalk<<<ww, kWalkThreads, smem_walk, st>>>(p);
+        ++launches;
     }
     timing_mark(3, st);
     k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(p);
@@ -1358,7 +1394,7 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
         sp.stage_cap = stage_cap_for((double) d[i].n_out / (double) d[i].n_units,
                                      sp.cfg.block_units);
         lay.n_sync += (sp.nreg + kSyncThreads - 1) / kSyncThreads;
-        if (sp.nreg > 1) lay.n_walk += (sp.nreg - 1 + kWalkThreads - 1) / kWalkThreads;
+        lay.n_walk += walk_ctas(sp.nreg);
         lay.smem_walk = std::max(lay.smem_walk, walk_smem(d[i].L));
         lay.n_scan += sp.ntiles;
         lay.n_final += (sp.nblk + kFinalThreads - 1) / kFinalThreads;
@@ -1504,8 +1540,9 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         p.nblk = (uint32_t) sp.nblk;
         p.nreg = (uint32_t) sp.nreg;
         p.stage_cap = sp.stage_cap;
+        p.wcap = walk_cap(sp.cfg);
         for (size_t r = 0; r < sp.nreg; r += kSyncThreads) b->items[is++] = {i, (uint32_t) r, 0, 0};
-        for (size_t r = 0; r + 1 < sp.nreg; r += kWalkThreads) b->items[iw++] = {i, (uint32_t) r, 0, 0};
+        for (uint32_t c = 0; c < walk_ctas(sp.nreg); ++c) b->items[iw++] = {i, c, 0, 0};
         for (size_t t = 0; t < sp.ntiles; ++t) b->items[ic++] = {i, (uint32_t) t, 0, 0};
         const uint32_t nctas = (uint32_t) ((sp.nblk + kFinalThreads - 1) / kFinalThreads);
         for (uint32_t c = 0; c < nctas; ++c) b->items[iff++] = {i, c, nctas, 0};
@@ -1562,16 +1599,14 @@ int mans_batch_decode(mans_batch* b, void* stream) {
     if (L.n_sync)
         k_gwalk_batch<<<(unsigned) L.n_sync, kSyncThreads, L.smem_sync, st>>>(ps, items);
     if (L.n_walk)
-        for (uint32_t pass = 1; pass <= kWalkPasses; ++pass)
-            k_wwalk_batch<<<(unsigned) L.n_walk, kWalkThreads, L.smem_walk, st>>>(
-                ps, items + L.n_sync, pass, kWalkWindows[pass - 1]);
+        k_wwalk_batch<<<(unsigned) L.n_walk, kWalkThreads, L.smem_walk, st>>>(ps, items + L.n_sync);
     if (L.n_scan)
         k_scan_batch<<<(unsigned) L.n_scan, kScanThreads, 0, st>>>(
             ps, items + L.n_sync + L.n_walk, (uint32_t*) (b->base + L.ticket));
     if (L.n_final)
         k_final_batch<<<(unsigned) L.n_final, kFinalThreads, L.smem_final, st>>>(
             ps, items + L.n_sync + L.n_walk + L.n_scan);
-    g_last_launches = 1 + (L.n_sync ? 1 : 0) + (L.n_walk ? kWalkPasses : 0) + (L.n_scan ? 1 : 0) +
+    g_last_launches = 1 + (L.n_sync ? 1 : 0) + (L.n_walk ? 1 : 0) + (L.n_scan ? 1 : 0) +
                       (L.n_final ? 1 : 0);
     return cudaGetLastError() == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
 }
