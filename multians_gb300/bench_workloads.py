@@ -54,9 +54,22 @@ def run_batched(args, ws, rank, local):
     gen_s = time.time() - t0
     total_sym = sum(st.n for st in sts)
     total_comp = sum(st.n_units * 4 for st in sts)
-    units = [torch.from_numpy(st.units.view(np.int32)).to(dev) for st in sts]
+    # all streams packed into one unit buffer (each stream 16-byte aligned)
+    # and one output buffer, as a caller batching many streams keeps them,
+    # so the host copies are one per direction
+    offs = np.zeros(len(sts) + 1, dtype=np.int64)
+    for i, st in enumerate(sts):
+        offs[i + 1] = offs[i] + ((st.units.size + 3) & ~3)
+    h_units_all = torch.zeros(int(offs[-1]), dtype=torch.int32).pin_memory()
+    hu_np = h_units_all.numpy()
+    for i, st in enumerate(sts):
+        hu_np[offs[i]: offs[i] + st.units.size] = st.units.view(np.int32)
+    d_units_all = h_units_all.to(dev)
+    units = [d_units_all[int(offs[i]): int(offs[i]) + st.units.size] for i, st in enumerate(sts)]
     tables = [torch.from_numpy(st.table.view(np.int32)).to(dev) for st in sts]
-    outs = [torch.empty(st.n, dtype=torch.uint8, device=dev) for st in sts]
+    oo = np.concatenate([[0], np.cumsum([st.n for st in sts])])
+    d_out_all = torch.empty(int(oo[-1]), dtype=torch.uint8, device=dev)
+    outs = [d_out_all[int(oo[i]): int(oo[i + 1])] for i in range(len(sts))]
     stream = torch.cuda.current_stream(dev)
 
     # batched decode
@@ -108,24 +121,26 @@ def run_batched(args, ws, rank, local):
     torch.cuda.synchronize(dev)
     loop_ms = l0.elapsed_time(l1) / lsteps
 
-    # e2e: host buffers -> device, graph decode, decoded bytes back
-    h_units = [torch.from_numpy(st.units.view(np.int32)).pin_memory() for st in sts]
-    h_out = [torch.empty(st.n, dtype=torch.uint8).pin_memory() for st in sts]
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for hu, u in zip(h_units, units):
-        u.copy_(hu, non_blocking=True)
-    b.graph_decode(stream)
-    for o, ho in zip(outs, h_out):
-        ho.copy_(o, non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    e2e_ms = e0.elapsed_time(e1)
+    # e2e: the packed host units -> device, graph decode, all symbols back
+    h_out_all = torch.empty(int(oo[-1]), dtype=torch.uint8).pin_memory()
+    e2e_times = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        d_out_all.fill_(0xCD)
+        e0.record(stream)
+        d_units_all.copy_(h_units_all, non_blocking=True)
+        b.graph_decode(stream)
+        h_out_all.copy_(d_out_all, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_times.append(e0.elapsed_time(e1))
+    e2e_ms = sorted(e2e_times)[1]
     if n_overflow:
         b.fixup(stream)
-        for o, ho in zip(outs, h_out):
-            ho.copy_(o)
-    e2e_ok = all(np.array_equal(ho.numpy()[::-1], st.symbols) for ho, st in zip(h_out, sts))
+        h_out_all.copy_(d_out_all)
+    ho_np = h_out_all.numpy()
+    e2e_ok = all(np.array_equal(ho_np[oo[i]: oo[i + 1]][::-1], st.symbols)
+                 for i, st in enumerate(sts))
     b.close()
     if rank != 0:
         return
@@ -155,7 +170,7 @@ def run_batched(args, ws, rank, local):
                      "alg_bytes_per_launch": total_comp + total_sym},
         "cpu_baseline": None,
         "e2e": {"value": round(ws * total_sym / (e2e_ms / 1e3) / 1e9, 3), "unit": "GB/s",
-                "h2d_bytes_per_step": total_comp, "d2h_bytes_per_step": total_sym,
+                "h2d_bytes_per_step": int(offs[-1]) * 4, "d2h_bytes_per_step": total_sym,
                 "bit_exact": bool(e2e_ok)},
         "gpu_launches": 4 * steps,
         "clocks": clk.summary(),
