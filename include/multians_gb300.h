@@ -50,13 +50,22 @@ typedef enum {
 int mans_status_code(uint32_t dev_status);
 
 /* Launch geometry of one decode.  Zero fields are chosen by the built-in
- * autotuner from (L, units, output size). */
+ * autotuner from (L, units, output size); flags are copied through. */
 typedef struct {
     uint32_t block_units;     /* units per output block (final pass) */
     uint32_t region_blocks;   /* blocks per sync region */
     uint32_t walk_slots;      /* regions a sync walk may cross */
     uint32_t threads;         /* threads per CTA */
+    uint32_t flags;           /* MANS_DECODE_* */
 } mans_cfg;
+
+/* Output order.  By default the output is in decode order, reversed like
+ * the reference's (src/main.cc:119-123: the caller reverses on the host).
+ * With MANS_DECODE_SOURCE_ORDER the final pass writes the i-th decoded
+ * symbol to out[n_out - 1 - i]: a full decode is then the source symbols
+ * in order and no host reversal is needed (CUHDOutputBuffer::reverse,
+ * src/multians_output_buffer.cc:27-29, fused into the write). */
+#define MANS_DECODE_SOURCE_ORDER 0x1u
 
 /* Fills `out` with the geometry the decoder uses for this call. */
 int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
@@ -137,7 +146,7 @@ typedef struct {
     uint32_t L;
     uint32_t first_state;
     uint32_t first_bit;
-    uint32_t reserved;
+    uint32_t flags;           /* MANS_DECODE_* */
 } mans_stream_desc;
 
 typedef struct mans_batch mans_batch;
@@ -192,7 +201,8 @@ typedef struct {
     uint32_t reserved[2];
 } mans_server_cfg;
 
-#define MANS_REQ_DEVICE_IO 0x1u   /* units / out are caller-owned device memory */
+#define MANS_REQ_DEVICE_IO 0x1u     /* units / out are caller-owned device memory */
+#define MANS_REQ_SOURCE_ORDER 0x2u  /* output in source order (MANS_DECODE_SOURCE_ORDER) */
 
 typedef struct {
     const uint32_t* units;    /* CUHDInputBuffer order; 16-byte aligned if device */

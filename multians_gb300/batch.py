@@ -13,7 +13,7 @@ class StreamDesc(ctypes.Structure):
                 ("d_out", ctypes.c_void_p), ("n_out", ctypes.c_uint64),
                 ("d_table", ctypes.c_void_p), ("L", ctypes.c_uint32),
                 ("first_state", ctypes.c_uint32), ("first_bit", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32)]
 
 
 def _sig():
@@ -38,12 +38,14 @@ def _sig():
     return L
 
 
-def desc(units, n_units, out, n_out, table, L, first_state, first_bit) -> StreamDesc:
-    """A stream descriptor from CUDA tensors (units/table int32 or uint32 views)."""
+def desc(units, n_units, out, n_out, table, L, first_state, first_bit,
+         source_order: bool = False) -> StreamDesc:
+    """A stream descriptor from CUDA tensors (units/table int32 or uint32
+    views); ``source_order`` writes the output in source order."""
     return StreamDesc(units.data_ptr() if units is not None else None, int(n_units),
                       out.data_ptr() if out is not None else None, int(n_out),
                       table.data_ptr() if table is not None else None, int(L),
-                      int(first_state), int(first_bit), 0)
+                      int(first_state), int(first_bit), 1 if source_order else 0)
 
 
 class Batch:

@@ -79,6 +79,7 @@ struct DecodeParams {
     uint32_t nreg;
     uint32_t stage_cap;    // staging bytes per warp in k_final (multiple of 16)
     uint32_t wcap;         // blocks a merge walk may run inside the G pass
+    uint32_t flags;        // MANS_DECODE_*
 };
 
 // Checks and converts the reference table, then builds both shared-memory
@@ -733,6 +734,7 @@ __device__ __forceinline__ void sts8(uint32_t a, uint32_t v) {
     asm volatile("st.shared.u8 [%0], %1;" :: "r"(a), "r"(v) : "memory");
 }
 
+template <bool kRev>
 __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, uint32_t nctas) {
     extern __shared__ __align__(16) uint2 s_tab[];
     load_prepared(s_tab, p.tab_sym, p.L);
@@ -809,8 +811,14 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
     const unsigned long long off_end = __shfl_sync(0xffffffffu, off_nx, last_lane);
     const unsigned long long lo = min(off0, p.n_out);
     const unsigned long long hi = min(max(off_end, off0), p.n_out);
-    const uint32_t phase = (uint32_t) (((uintptr_t) p.out + off0) & 15u);
-    const bool staged = hi - lo + phase <= p.stage_cap;
+    // the warp writes output indices [wlo, whi): decode indices [lo, hi), or
+    // in source order their mirror images n_out - 1 - i; the staging buffer
+    // holds output index j at byte sb + (j - wlo), with the output's 16-byte
+    // phase
+    const unsigned long long wlo = kRev ? p.n_out - hi : lo;
+    const unsigned long long whi = kRev ? p.n_out - lo : hi;
+    const uint32_t sb = (uint32_t) (((uintptr_t) p.out + wlo) & 15u);
+    const bool staged = whi - wlo + sb <= p.stage_cap;
 
     // every lane's range must lie inside the warp's range (offsets are
     // monotonic in the block index); anything else is reported, not written
@@ -833,10 +841,10 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
         const UnitSrc ts{tile, u0, ~0u, tile_units - 1};
         const uint64_t bs = (uint64_t) b * p.B * 32;   // cursor units are global indices
         c.init(ts, bs, bs + rel, tb + 8u * idx);
-        if (staged) {
+        if (staged && !kRev) {
             // bytes up to a word boundary, then four symbols per 32-bit
             // store, then the remaining bytes
-            uint32_t q = stage_addr + phase + (uint32_t) (off - off0);
+            uint32_t q = stage_addr + sb + (uint32_t) (off - wlo);
             uint32_t i = 0;
             for (; i < cnt && (q & 3u) && c.pos < pos_cap; ++i, ++q)
                 sts8(q, c.step(ts) >> 24);
@@ -849,36 +857,58 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
             }
             for (; i < cnt && c.pos < pos_cap; ++i, ++q)
                 sts8(q, c.step(ts) >> 24);
-        } else {
+        } else if (staged) {
+            // source order: decode index i goes to output n_out - 1 - i, so
+            // the lane fills its staging bytes downwards, four symbols per
+            // 32-bit store once the address is the top byte of a word
+            uint32_t q = stage_addr + sb + (uint32_t) (p.n_out - 1 - off - wlo);
+            uint32_t i = 0;
+            for (; i < cnt && (q & 3u) != 3u && c.pos < pos_cap; ++i, --q)
+                sts8(q, c.step(ts) >> 24);
+            for (; i + 4 <= cnt && c.pos < pos_cap; i += 4, q -= 4) {
+                const uint32_t y0 = c.step(ts), y1 = c.step(ts);
+                const uint32_t y2 = c.step(ts), y3 = c.step(ts);
+                const uint32_t lo2 = __byte_perm(y3, y2, 0x0073);   // sym3 | sym2 << 8
+                const uint32_t hi2 = __byte_perm(y1, y0, 0x7300);   // sym1 << 16 | sym0 << 24
+                sts32(q - 3, __byte_perm(lo2, hi2, 0x7610));
+            }
+            for (; i < cnt && c.pos < pos_cap; ++i, --q)
+                sts8(q, c.step(ts) >> 24);
+        } else if (!kRev) {
             uint8_t* dst = p.out + off;
             for (uint32_t i = 0; i < cnt && c.pos < pos_cap; ++i)
                 dst[i] = (uint8_t) (c.step(ts) >> 24);
+        } else {
+            uint8_t* dst = p.out + (p.n_out - 1 - off);
+            for (uint32_t i = 0; i < cnt && c.pos < pos_cap; ++i)
+                *(dst - i) = (uint8_t) (c.step(ts) >> 24);
         }
         // a block decoded to its full count ends at the next block start
         if (cnt == full && b + 1 < p.nblk &&
             (c.pos < p.B * 32 || c.pos >= p.B * 32 + kMaxBits + 1))
             atomicOr(p.status, MANS_DEV_COUNT_MISMATCH);
     }
-    if (!staged || lo >= hi) return;
+    if (!staged || wlo >= whi) return;
     __syncwarp();
-    // [lo, hi) from stage[phase + (i - off0)]; aligned middle in 16 B words
+    // [wlo, whi) from stage[sb + (j - wlo)]; aligned middle in 16 B words
     const uint8_t* stage = reinterpret_cast<const uint8_t*>(s_tab) + (stage_addr - tb);
     const uintptr_t base = (uintptr_t) p.out;
-    unsigned long long a0 = lo + ((16 - ((base + lo) & 15)) & 15);
-    unsigned long long a1 = hi - ((base + hi) & 15);
-    if (a0 > a1) a0 = a1 = hi;
-    for (unsigned long long i = lo + lane; i < a0; i += 32)
-        p.out[i] = stage[phase + (i - off0)];
-    for (unsigned long long i = a1 + lane; i < hi; i += 32)
-        p.out[i] = stage[phase + (i - off0)];
-    const uint4* src = reinterpret_cast<const uint4*>(stage + phase + (a0 - off0));
+    unsigned long long a0 = wlo + ((16 - ((base + wlo) & 15)) & 15);
+    unsigned long long a1 = whi - ((base + whi) & 15);
+    if (a0 > a1) a0 = a1 = whi;
+    for (unsigned long long i = wlo + lane; i < a0; i += 32)
+        p.out[i] = stage[sb + (i - wlo)];
+    for (unsigned long long i = a1 + lane; i < whi; i += 32)
+        p.out[i] = stage[sb + (i - wlo)];
+    const uint4* src = reinterpret_cast<const uint4*>(stage + sb + (a0 - wlo));
     uint4* dst = reinterpret_cast<uint4*>(p.out + a0);
     const uint32_t nvec = (uint32_t) ((a1 - a0) >> 4);
     for (uint32_t v = lane; v < nvec; v += 32) dst[v] = src[v];
 }
 
+template <bool kRev>
 __global__ void __launch_bounds__(kFinalThreads) k_final(DecodeParams p) {
-    final_body(p, blockIdx.x, gridDim.x);
+    final_body<kRev>(p, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -944,7 +974,8 @@ __global__ void __launch_bounds__(kFinalThreads) k_final_batch(const DecodeParam
     __shared__ DecodeParams sp;
     const BatchItem it = items[blockIdx.x];
     load_params(sp, ps + it.stream);
-    final_body(sp, it.index, it.count);
+    if (sp.flags & MANS_DECODE_SOURCE_ORDER) final_body<true>(sp, it.index, it.count);
+    else final_body<false>(sp, it.index, it.count);
 }
 
 // ---------------------------------------------------------------------------
@@ -989,7 +1020,8 @@ static void set_kernel_attributes() {
     cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_gwalk, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_wwalk, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_final, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_final<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_final<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_prep_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_gwalk_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_wwalk_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
@@ -1209,6 +1241,7 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     p.nblk = (uint32_t) nblk;
     p.nreg = (uint32_t) nreg;
     p.wcap = walk_cap(cfg);
+    p.flags = cfg.flags & MANS_DECODE_SOURCE_ORDER;
 
     const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
     if (cudaMemsetAsync(p.status, 0, sizeof(uint32_t), st) != cudaSuccess ||
@@ -1241,7 +1274,9 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     timing_mark(3, st);
     k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(p);
     timing_mark(4, st);
-    k_final<<<(unsigned) ((nblk + kFinalThreads - 1) / kFinalThreads), kFinalThreads, smem_final, st>>>(p);
+    const unsigned gf = (unsigned) ((nblk + kFinalThreads - 1) / kFinalThreads);
+    if (p.flags & MANS_DECODE_SOURCE_ORDER) k_final<true><<<gf, kFinalThreads, smem_final, st>>>(p);
+    else k_final<false><<<gf, kFinalThreads, smem_final, st>>>(p);
     timing_mark(5, st);
     if (g_timing.on && g_timing.used < g_timing.cap) ++g_timing.used;
     g_last_launches = launches;
@@ -1384,6 +1419,7 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
             return MANS_ERR_ARG;
         int rc = mans_plan(d[i].n_units, d[i].n_out, d[i].L, hint, &sp.cfg);
         if (rc != MANS_OK) return rc;
+        sp.cfg.flags = d[i].flags & MANS_DECODE_SOURCE_ORDER;
         sp.nblk = num_blocks(d[i].n_units, sp.cfg.block_units);
         sp.nreg = (sp.nblk + sp.cfg.region_blocks - 1) / sp.cfg.region_blocks;
         sp.ntiles = (sp.nreg + kScanTile - 1) / kScanTile;
@@ -1541,6 +1577,7 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         p.nreg = (uint32_t) sp.nreg;
         p.stage_cap = sp.stage_cap;
         p.wcap = walk_cap(sp.cfg);
+        p.flags = d.flags & MANS_DECODE_SOURCE_ORDER;
         for (size_t r = 0; r < sp.nreg; r += kSyncThreads) b->items[is++] = {i, (uint32_t) r, 0, 0};
         for (uint32_t c = 0; c < walk_ctas(sp.nreg); ++c) b->items[iw++] = {i, c, 0, 0};
         for (size_t t = 0; t < sp.ntiles; ++t) b->items[ic++] = {i, (uint32_t) t, 0, 0};

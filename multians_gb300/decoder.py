@@ -107,11 +107,18 @@ def aux_status(aux, stream=None) -> int:
 
 
 def decode(units, n_units: int, n_out: int, table, first_state: int, first_bit: int,
-           L: int | None = None, aux=None, out=None, stream=None, cfg: dict | None = None):
-    """Decodes one stream and returns the symbols (decode order, CUDA uint8).
+           L: int | None = None, aux=None, out=None, stream=None, cfg: dict | None = None,
+           source_order: bool = False):
+    """Decodes one stream and returns the symbols (CUDA uint8): in decode
+    order like the reference, or with ``source_order`` the i-th decoded
+    symbol at out[n_out - 1 - i] (a full decode is then the source).
 
     ``units``/``table`` may be numpy arrays (copied to the device) or CUDA
     tensors."""
+    if source_order:
+        from ._lib import DECODE_SOURCE_ORDER
+        cfg = dict(cfg or {})
+        cfg["flags"] = cfg.get("flags", 0) | DECODE_SOURCE_ORDER
     torch = _torch()
     dev = torch.device("cuda")
     if not hasattr(units, "is_cuda"):

@@ -98,3 +98,24 @@ def test_batch_per_stream_status_and_special_streams(mg, oracle_lib):
         assert np.array_equal(o[: st.n].cpu().numpy()[::-1], st.symbols)
     assert bool((oo == 42).all())
     b.close()
+
+
+def test_batch_mixed_output_orders(mg):
+    """Streams of one batch choose their output order independently."""
+    import torch
+
+    from multians_gb300 import batch, host
+    specs = [(41 + i, (0.05, 0.7, 2.0)[i % 3], 50_000 + 9_973 * i, (1024, 4096)[i % 2])
+             for i in range(12)]
+    streams = _streams(host, specs)
+    descs = [batch.desc(u, st.n_units, o, st.n, t, st.L, st.first_state, st.first_bit,
+                        source_order=bool(i % 2))
+             for i, (st, u, t, o) in enumerate(streams)]
+    b = batch.Batch(descs)
+    s = torch.cuda.current_stream()
+    b.graph_decode(s)
+    assert b.status(s)[0] == 0
+    for i, (st, u, t, o) in enumerate(streams):
+        got = o[: st.n].cpu().numpy()
+        assert np.array_equal(got if i % 2 else got[::-1], st.symbols), i
+    b.close()

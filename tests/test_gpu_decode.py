@@ -170,3 +170,28 @@ def test_bad_table_rejected(mg, oracle_lib):
     with pytest.raises(mg.MansError):
         mg.decode(_dev(st.units), st.n_units, st.n, _dev(bad), st.first_state, st.first_bit,
                   L=st.L, out=out)
+
+
+@pytest.mark.parametrize("L,lam", [(1024, 0.05), (1024, 2.0), (4096, 0.005), (4096, 1.0)])
+@pytest.mark.parametrize("shift", [0, 3, 13])
+def test_source_order_output(mg, oracle_lib, L, lam, shift):
+    """MANS_DECODE_SOURCE_ORDER: the final pass writes the i-th decoded
+    symbol to out[n_out - 1 - i], at any output alignment; full decodes give
+    the source, short ones the mirrored prefix."""
+    import torch
+    O = oracle_lib
+    st = O.make_stream(seed=300 + L + int(lam * 100), lam=lam, n=200_003, L=L)
+    units, table = _dev(st.units), _dev(st.table)
+    big = torch.full((st.n + 64,), 0xCD, dtype=torch.uint8, device="cuda")
+    out = big[shift: shift + st.n]
+    mg.decode(units, st.n_units, st.n, table, st.first_state, st.first_bit, L=L, out=out,
+              source_order=True)
+    assert np.array_equal(out.cpu().numpy(), st.symbols)
+    b = big.cpu().numpy()
+    assert (b[:shift] == 0xCD).all() and (b[shift + st.n:] == 0xCD).all()
+    want = O.decode_seq(st)
+    for short in (1, 4097, st.n - 7):
+        o2 = torch.full((short,), 0xCD, dtype=torch.uint8, device="cuda")
+        mg.decode(units, st.n_units, short, table, st.first_state, st.first_bit, L=L, out=o2,
+                  source_order=True)
+        assert np.array_equal(o2.cpu().numpy(), want[:short][::-1]), short

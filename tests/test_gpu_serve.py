@@ -160,3 +160,22 @@ def test_device_io_pageable_and_errors(mg):
         bad[3] = (bad[3] & 0x00FFFFFF) | (20 << 24)
         with pytest.raises(mg.MansError):
             srv.add_table(bad)
+
+
+def test_source_order_requests(mg):
+    """A request can ask for its output in source order; others in the same
+    launch keep decode order."""
+    from multians_gb300 import serve
+    pool = _pool(6, seed=23, max_sym=300_000)
+    with serve.Server(budget_bytes=512 << 20) as srv:
+        items = _setup(srv, pool)
+        reqs = []
+        for i, (st, tid, units, out) in enumerate(items):
+            reqs.append(serve.request(units, st.n_units, out, st.n, tid, st.first_state,
+                                      st.first_bit, tag=i, source_order=bool(i % 2)))
+        srv.submit(reqs)
+        done = srv.wait(len(reqs))
+        assert all(c.status == 0 for c in done)
+        for i, (st, _, _, out) in enumerate(items):
+            got = out.numpy()
+            assert np.array_equal(got if i % 2 else got[::-1], st.symbols), i
