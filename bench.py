@@ -1,7 +1,7 @@
 """Benchmark of the MULTIANS decode path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload plain|batched|served] [--mb 256] [--lam 0.05] [--L 1024]
+                    [--workload plain|batched|served|encode] [--mb 256] [--lam 0.05] [--L 1024]
 
 One JSON line on stdout (rank 0).  The default workload is the plain
 single-stream decode of a 256 MB stream (lambda = 0.05, L = 1024 states):
@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["plain", "batched", "served"], default="plain")
+    ap.add_argument("--workload", choices=["plain", "batched", "served", "encode"], default="plain")
     ap.add_argument("--mb", type=float, default=256.0, help="stream size in MiB of symbols")
     ap.add_argument("--lam", type=float, default=0.05)
     ap.add_argument("--L", type=int, default=1024)

@@ -49,6 +49,9 @@ public:
                                               std::function<double(double)> fun);
     static Distribution generate_distribution_from_buffer(size_t seed, size_t N,
                                                           std::uint8_t* in, size_t size);
+    // Not in the reference: the same distribution from a byte histogram.
+    static Distribution generate_distribution_from_histogram(size_t seed, size_t N,
+                                                             const std::uint64_t* hist);
     static std::shared_ptr<std::vector<SYMBOL_TYPE>> generate_test_data(
         std::shared_ptr<std::vector<size_t>> distr, size_t size, size_t num_states, size_t seed);
     static std::shared_ptr<std::vector<std::vector<Encoder_Table_Entry>>> generate_table(

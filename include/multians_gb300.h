@@ -267,6 +267,42 @@ int mans_host_encode(const uint8_t* sym, size_t n, uint32_t L, uint32_t table_se
                      uint32_t* dec_table, uint32_t* units, size_t cap, size_t* n_units,
                      uint32_t* first_bit, uint32_t* first_state);
 
+/* GPU encoder: the reference's table build and ANSEncoder::encode
+ * (src/ans_table_generator.cc:61-314, src/ans_encoder.cc:13-97) with the
+ * counting and the encoding on the device.  The units equal the host
+ * encoder's (mans_host_encode) bit for bit, in CUHDInputBuffer order with
+ * four zero units of padding; the byte after the last symbol is taken as 0
+ * (mans_host_encode reads it from the zero padding it adds).  L must be a
+ * power of two <= 8192.
+ *   mans_histogram          byte counts of d_sym into d_hist[256] (async)
+ *   mans_host_encode_tables tables from those counts: the L-word decoder
+ *                           table and the encoder table blob
+ *                           (mans_encode_blob_words words)
+ *   mans_encode             encodes n bytes (d_sym 16-byte aligned) into
+ *                           d_units (mans_encode_max_units words); workspace
+ *                           mans_encode_aux_size bytes; chunk_hint 0 = plan
+ *                           (async)
+ *   mans_encode_result      n_units, first_bit, first_state (synchronous);
+ *                           MANS_ERR_SYNC: merges ran out of slots, retry
+ *                           with a larger chunk_hint */
+size_t mans_encode_blob_words(uint32_t L);
+int mans_histogram(const uint8_t* d_sym, size_t n, uint64_t* d_hist, void* stream);
+int mans_host_encode_tables(const uint64_t* hist, uint32_t L, uint32_t table_seed,
+                            uint32_t* dec_table, uint32_t* enc_blob);
+size_t mans_encode_max_units(size_t n, uint32_t L);
+size_t mans_encode_aux_size(size_t n, uint32_t chunk_hint);
+int mans_encode(const uint8_t* d_sym, size_t n, const uint32_t* d_enc_blob, uint32_t L,
+                uint32_t* d_units, size_t cap_units, void* d_aux, size_t aux_bytes,
+                uint32_t chunk_hint, void* stream);
+int mans_encode_result(const void* d_aux, void* stream, uint64_t* n_units, uint32_t* first_bit,
+                       uint32_t* first_state, uint32_t* dev_status);
+/* mans_encode + mans_encode_result, re-planning with 4x longer chunks while
+ * the merges outrun their slots (workspace: mans_encode_aux_size(n, 0)). */
+int mans_encode_sync(const uint8_t* d_sym, size_t n, const uint32_t* d_enc_blob, uint32_t L,
+                     uint32_t* d_units, size_t cap_units, void* d_aux, size_t aux_bytes,
+                     void* stream, uint64_t* n_units, uint32_t* first_bit,
+                     uint32_t* first_state);
+
 /* Decode that allocates nothing.  No counterpart in the reference: its
  * decode needs caller-allocated CUHDGPUDecoderMemory.  For callers that may
  * not allocate device memory when they decode (inside a host application's

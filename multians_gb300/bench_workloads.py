@@ -179,7 +179,83 @@ def run_batched(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def run_encode(args, ws, rank, local):
+    """GPU encode of the plain workload's stream (256 MiB, lambda, L): value =
+    encoded source bytes per second with the symbols resident in HBM
+    (histogram, table build from it on the host, encode); e2e adds the
+    symbols' host->device copy and the units' copy back.  The units are
+    checked against the host encoder's.  cpu_baseline: the host encoder
+    (the reference's ANSEncoder restated) on a bounded prefix."""
+    import torch
+
+    from multians_gb300 import encode, host
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n = int(args.mb * (1 << 20))
+    sym = host.gen_symbols(args.seed + rank, args.lam, n)
+    h_sym = torch.from_numpy(sym).pin_memory()
+    d_sym = h_sym.to(dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(3, args.warmup)):
+        units, n_units, fb, fs, dec = encode.encode(d_sym, args.L)
+    torch.cuda.synchronize(dev)
+    steps = max(3, args.steps)
+    from bench import ClockSampler
+    t_dev = []
+    with ClockSampler(local) as clk:
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            units, n_units, fb, fs, dec = encode.encode(d_sym, args.L)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            t_dev.append(e0.elapsed_time(e1))
+    # e2e: symbols in from pinned host memory, units back
+    h_units = torch.empty(units.numel(), dtype=torch.int32).pin_memory()
+    t_e2e = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        d2 = h_sym.to(dev, non_blocking=True)
+        u2, nu2, fb2, fs2, _ = encode.encode(d2, args.L)
+        h_units[: u2.numel()].copy_(u2, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        t_e2e.append(e0.elapsed_time(e1))
+    # parity with the host encoder (full stream) and its time on a prefix
+    t0 = time.perf_counter()
+    ref = host.encode(sym, args.L)
+    host_s = time.perf_counter() - t0
+    exact = (n_units, fb, fs) == (ref.n_units, ref.first_bit, ref.first_state) and bool(
+        np.array_equal(units.cpu().numpy().view(np.uint32), ref.units))
+    if rank != 0:
+        return
+    ms = statistics.median(t_dev)
+    line = {
+        "metric": "encoded GB/s on 1 GB300 (source bytes / s), bit-exact with the reference encoder",
+        "value": round(ws * n / (ms / 1e3) / 1e9, 3), "unit": "GB/s", "n_gpus": ws,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic",
+        "config": {"workload": f"encode {args.mb:g}MiB lambda={args.lam} L={args.L}",
+                   "n_symbols": n, "n_units": n_units, "seed": args.seed,
+                   "step": "histogram + host table build + 6 encode kernels"},
+        "bit_exact": exact,
+        "e2e": {"value": round(ws * n / (statistics.median(t_e2e) / 1e3) / 1e9, 3),
+                "unit": "GB/s", "h2d_bytes_per_step": n, "d2h_bytes_per_step": int(u2.numel()) * 4},
+        "cpu_baseline": {"value": round(n / host_s / 1e9, 4), "unit": "GB/s", "cores": 1,
+                         "kind": "port", "sample": "the whole stream, the library's host encoder "
+                                                   "(the reference's ANSEncoder restated), one core"},
+        "gpu_launches": 8 * steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run(args, ws, rank, local):
+    if args.workload == "encode":
+        return run_encode(args, ws, rank, local)
     if args.workload == "batched":
         return run_batched(args, ws, rank, local)
     if args.workload == "served":

@@ -156,11 +156,19 @@ Distribution ANSTableGenerator::generate_distribution(size_t seed, size_t n, siz
 Distribution ANSTableGenerator::generate_distribution_from_buffer(size_t seed, size_t N,
                                                                   std::uint8_t* in,
                                                                   size_t size) {
-    std::array<std::uint32_t, 256> hist{};
+    std::array<std::uint64_t, 256> hist{};
     for (size_t i = 0; i < size; ++i) ++hist[in[i]];
+    return generate_distribution_from_histogram(seed, N, hist.data());
+}
+
+// The distribution depends on the buffer only through its byte histogram
+// (src/ans_table_generator.cc:61-100 counts, then normalises), so a
+// histogram taken elsewhere (on the GPU) gives the same table.
+Distribution ANSTableGenerator::generate_distribution_from_histogram(size_t seed, size_t N,
+                                                                     const std::uint64_t* hist) {
     std::vector<size_t> counts;
     std::vector<SYMBOL_TYPE> symbols;
-    for (size_t v = 0; v < hist.size(); ++v) {
+    for (size_t v = 0; v < 256; ++v) {
         if (hist[v]) {
             counts.push_back(hist[v]);
             symbols.push_back((SYMBOL_TYPE) v);
@@ -399,6 +407,63 @@ std::shared_ptr<ANSEncoderTable> tables_for(const uint8_t* sym, size_t n, uint32
 size_t mans_host_max_units(const uint8_t* sym, size_t n, uint32_t L, uint32_t table_seed) {
     if (!sym || n == 0 || L < 2) return 0;
     return ANSTableGenerator::get_max_compressed_size(tables_for(sym, n, L, table_seed), n) + 4;
+}
+
+int mans_host_encode_tables(const uint64_t* hist, uint32_t L, uint32_t table_seed,
+                            uint32_t* dec_table, uint32_t* enc_blob) {
+    if (!hist || !dec_table || !enc_blob || L < 2 || L > 8192 || (L & (L - 1)) != 0)
+        return MANS_ERR_ARG;
+    uint64_t n = 0;
+    for (int v = 0; v < 256; ++v) n += hist[v];
+    if (n == 0) return MANS_ERR_ARG;
+    auto d = ANSTableGenerator::generate_distribution_from_histogram(table_seed, L, hist);
+    auto t = ANSTableGenerator::generate_table(d.prob, d.dist, d.symbols, d.symbols->size(), L);
+    auto enc = ANSTableGenerator::generate_encoder_table(t);
+    auto dec = ANSTableGenerator::get_decoder_table(enc);
+    std::memcpy(dec_table, dec->get(), (size_t) L * sizeof(uint32_t));
+    // Compact encoder table (the encoder kernels' format).  Encoding byte s
+    // from state X in [L, 2L) shifts out k low bits with (X >> k) in
+    // [f, 2f) (f = the byte's normalised count) and moves to the spread
+    // state of (s, X >> k).  With L = 2^R and m = R + 1 - bitlength(f - 1),
+    // k = (X + delta) >> 16 for delta = (m << 16) - (f << m); the next state
+    // is next[base + (X >> k)] with base = (first slot of s) - f.
+    //   words 0..511: per byte {delta, base} (base = ~0: byte absent)
+    //   then L / 2 words: next states as uint16 (L + spread index)
+    const size_t K = d.symbols->size();
+    uint32_t lg = 0;
+    while ((1u << lg) < L) ++lg;
+    std::vector<uint32_t> first(256, 0), cnt(256, 0);
+    uint32_t slot = 0;
+    for (size_t i = 0; i < K; ++i) {
+        const SYMBOL_TYPE sv = d.symbols->at(i);
+        cnt[sv] = (uint32_t) d.dist->at(i);
+        first[sv] = slot;
+        slot += cnt[sv];
+    }
+    if (slot != L) return MANS_ERR_TABLE;
+    for (int v = 0; v < 256; ++v) {
+        if (cnt[v] == 0) {
+            enc_blob[2 * v] = 0;
+            enc_blob[2 * v + 1] = ~0u;
+            continue;
+        }
+        uint32_t bl = 0;
+        while (bl < 32 && ((cnt[v] - 1) >> bl) != 0) ++bl;
+        const uint32_t m = lg + 1 - bl;
+        enc_blob[2 * v] = (m << 16) - (cnt[v] << m);
+        enc_blob[2 * v + 1] = first[v] - cnt[v];
+    }
+    uint16_t* next = reinterpret_cast<uint16_t*>(enc_blob + 512);
+    for (int v = 0; v < 256; ++v) {
+        if (cnt[v] == 0) continue;
+        const auto& row = enc->table[v];
+        for (uint32_t X = L; X < 2 * L; ++X) {
+            const auto& e = row[X - L];
+            const uint32_t xs = X >> e.code_length;
+            next[first[v] + xs - cnt[v]] = (uint16_t) e.next_state;
+        }
+    }
+    return MANS_OK;
 }
 
 int mans_host_encode(const uint8_t* sym, size_t n, uint32_t L, uint32_t table_seed,
