@@ -203,6 +203,9 @@ typedef struct {
 
 #define MANS_REQ_DEVICE_IO 0x1u     /* units / out are caller-owned device memory */
 #define MANS_REQ_SOURCE_ORDER 0x2u  /* output in source order (MANS_DECODE_SOURCE_ORDER) */
+#define MANS_REQ_CONTAINER 0x4u     /* units points at a host container of n_units
+                                       bytes; table, n_out, first_state / first_bit
+                                       come from it (out must hold n_symbols) */
 
 typedef struct {
     const uint32_t* units;    /* CUHDInputBuffer order; 16-byte aligned if device */
@@ -302,6 +305,24 @@ int mans_encode_sync(const uint8_t* d_sym, size_t n, const uint32_t* d_enc_blob,
                      uint32_t* d_units, size_t cap_units, void* d_aux, size_t aux_bytes,
                      void* stream, uint64_t* n_units, uint32_t* first_bit,
                      uint32_t* first_state);
+
+/* Stream container: one buffer holding a 64-byte header (magic, symbol and
+ * unit counts, L, first state and bit, a header checksum), the L-word
+ * decoder table and the units in CUHDInputBuffer order (no padding).  The
+ * reference passes these as separate arguments (src/main.cc:111-116).
+ * mans_container_parse checks the header and bounds and reports where the
+ * table and units start; it does not read the payload. */
+typedef struct {
+    uint64_t n_symbols, n_units;
+    uint32_t L, first_state, first_bit, reserved;
+    uint64_t table_offset, units_offset;   /* bytes from the buffer start */
+} mans_container_info;
+
+size_t mans_container_size(uint64_t n_units, uint32_t L);
+int mans_container_write(void* buf, size_t cap, const uint32_t* units, uint64_t n_units,
+                         uint64_t n_symbols, const uint32_t* table, uint32_t L,
+                         uint32_t first_state, uint32_t first_bit, size_t* size);
+int mans_container_parse(const void* buf, size_t size, mans_container_info* info);
 
 /* Decode that allocates nothing.  No counterpart in the reference: its
  * decode needs caller-allocated CUHDGPUDecoderMemory.  For callers that may

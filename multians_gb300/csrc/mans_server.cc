@@ -35,6 +35,7 @@
 #include <deque>
 #include <memory>
 #include <mutex>
+#include <unordered_map>
 #include <thread>
 #include <vector>
 
@@ -68,7 +69,18 @@ bool is_pinned_host(const void* p) {
 struct Table {
     uint64_t off;
     uint32_t L;
+    uint64_t hash;                 // FNV-1a of the words, for container lookups
+    std::vector<uint32_t> words;   // host copy
 };
+
+uint64_t table_hash(const uint32_t* t, uint32_t L) {
+    uint64_t h = 1469598103934665603ull ^ L;
+    for (uint32_t j = 0; j < L; ++j) {
+        h ^= t[j];
+        h *= 1099511628211ull;
+    }
+    return h;
+}
 
 struct Req {
     mans_request r;
@@ -103,7 +115,41 @@ struct mans_server {
     mans::Arena arena;
     std::mutex arena_mu;
     std::vector<Table> tables;
+    std::unordered_multimap<uint64_t, uint32_t> table_ids;   // hash -> id
     std::mutex tables_mu;
+
+    // Adds a table (or finds the identical one already resident).
+    int add_table(const uint32_t* host_table, uint32_t L, uint32_t* id) {
+        if (mans_table_check(host_table, L) < 0) return MANS_ERR_TABLE;
+        const uint64_t h = table_hash(host_table, L);
+        {
+            std::lock_guard<std::mutex> lk(tables_mu);
+            auto range = table_ids.equal_range(h);
+            for (auto it = range.first; it != range.second; ++it) {
+                const Table& t = tables[it->second];
+                if (t.L == L && std::memcmp(t.words.data(), host_table, (size_t) L * 4) == 0) {
+                    *id = it->second;
+                    return MANS_OK;
+                }
+            }
+        }
+        uint64_t off;
+        {
+            std::lock_guard<std::mutex> lk(arena_mu);
+            if (!arena.alloc((uint64_t) L * 4, &off)) return MANS_ERR_NOMEM;
+        }
+        if (cudaMemcpy(base + off, host_table, (size_t) L * 4, cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+            std::lock_guard<std::mutex> lk(arena_mu);
+            arena.release(off);
+            return MANS_ERR_CUDA;
+        }
+        std::lock_guard<std::mutex> lk(tables_mu);
+        *id = (uint32_t) tables.size();
+        tables.push_back({off, L, h, std::vector<uint32_t>(host_table, host_table + L)});
+        table_ids.emplace(h, *id);
+        return MANS_OK;
+    }
 
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_ev = nullptr;
@@ -155,8 +201,26 @@ struct mans_server {
         delete q;
     }
 
-    // Checks a request and sizes its device block.
+    // Checks a request and sizes its device block.  A container request
+    // gets its stream fields (and table) from the container header.
     int validate(Req* q) {
+        if (q->r.flags & MANS_REQ_CONTAINER) {
+            if (q->r.flags & MANS_REQ_DEVICE_IO) return MANS_ERR_ARG;
+            mans_container_info ci;
+            const int rc = mans_container_parse(q->r.units, q->r.n_units, &ci);
+            if (rc != MANS_OK) return rc;
+            if (ci.n_symbols > q->r.n_out) return MANS_ERR_ARG;
+            const unsigned char* c = (const unsigned char*) q->r.units;
+            uint32_t tid = 0;
+            const int tr = add_table((const uint32_t*) (c + ci.table_offset), ci.L, &tid);
+            if (tr != MANS_OK) return tr;
+            q->r.units = (const uint32_t*) (c + ci.units_offset);
+            q->r.n_units = ci.n_units;
+            q->r.n_out = ci.n_symbols;
+            q->r.table = tid;
+            q->r.first_state = ci.first_state;
+            q->r.first_bit = ci.first_bit;
+        }
         const mans_request& r = q->r;
         uint32_t L;
         uint64_t toff;
@@ -493,22 +557,7 @@ int mans_server_create(const mans_server_cfg* cfg, mans_server** out) {
 
 int mans_server_add_table(mans_server* s, const uint32_t* host_table, uint32_t L, uint32_t* id) {
     if (!s || !host_table || !id || L < 2 || L > 8192) return MANS_ERR_ARG;
-    if (mans_table_check(host_table, L) < 0) return MANS_ERR_TABLE;
-    uint64_t off;
-    {
-        std::lock_guard<std::mutex> lk(s->arena_mu);
-        if (!s->arena.alloc((uint64_t) L * 4, &off)) return MANS_ERR_NOMEM;
-    }
-    if (cudaMemcpy(s->base + off, host_table, (size_t) L * 4, cudaMemcpyHostToDevice) !=
-        cudaSuccess) {
-        std::lock_guard<std::mutex> lk(s->arena_mu);
-        s->arena.release(off);
-        return MANS_ERR_CUDA;
-    }
-    std::lock_guard<std::mutex> lk(s->tables_mu);
-    *id = (uint32_t) s->tables.size();
-    s->tables.push_back({off, L});
-    return MANS_OK;
+    return s->add_table(host_table, L, id);
 }
 
 int mans_server_submit(mans_server* s, const mans_request* reqs, size_t n) {

@@ -20,6 +20,7 @@ from ._lib import MansError, check, lib
 
 REQ_DEVICE_IO = 0x1
 REQ_SOURCE_ORDER = 0x2
+REQ_CONTAINER = 0x4
 
 
 class ServerCfg(ctypes.Structure):
@@ -93,6 +94,17 @@ def request(units, n_units, out, n_out, table, first_state, first_bit, tag=0,
     flags = (REQ_DEVICE_IO if device_io else 0) | (REQ_SOURCE_ORDER if source_order else 0)
     return RequestC(up, int(n_units), op, int(n_out), int(table), int(first_state),
                     int(first_bit), flags, int(tag), int(arrival_ns))
+
+
+def request_container(container, out, tag=0, arrival_ns=0, source_order=False) -> RequestC:
+    """A request whose stream, table and parameters come from a host
+    container (multians_gb300.container); `out` holds at least its symbols."""
+    cp = container if isinstance(container, int) else container.data_ptr()
+    nbytes = container.numel() * container.element_size()
+    op = out if isinstance(out, int) else out.data_ptr()
+    n_out = out.numel() if hasattr(out, "numel") else 0
+    flags = REQ_CONTAINER | (REQ_SOURCE_ORDER if source_order else 0)
+    return RequestC(cp, int(nbytes), op, int(n_out), 0, 0, 0, flags, int(tag), int(arrival_ns))
 
 
 class Server:

@@ -179,3 +179,32 @@ def test_source_order_requests(mg):
         for i, (st, _, _, out) in enumerate(items):
             got = out.numpy()
             assert np.array_equal(got if i % 2 else got[::-1], st.symbols), i
+
+
+def test_container_requests_share_resident_tables(mg):
+    """Requests given as containers: the server reads the stream parameters
+    from the header and adds each distinct table once."""
+    import torch
+
+    from multians_gb300 import container, host, serve
+    a = host.make_stream(71, 0.05, 150_000, 1024)
+    b = host.encode(host.gen_symbols(72, 0.05, 90_000), 1024)
+    with serve.Server(budget_bytes=256 << 20) as srv:
+        outs, bufs = [], []
+        for i, st in enumerate((a, a, b)):
+            c = torch.from_numpy(container.pack_encoded(st)).pin_memory()
+            o = torch.full((st.n + 5,), 0xCD, dtype=torch.uint8).pin_memory()
+            bufs.append(c)
+            outs.append(o)
+            srv.submit([serve.request_container(c, o, tag=i, source_order=(i == 2))])
+            (done,) = srv.wait(1)
+            assert done.status == 0, done
+        base = srv.stats()["range_in_use"]
+        assert np.array_equal(outs[0].numpy()[: a.n][::-1], a.symbols)
+        assert np.array_equal(outs[1].numpy()[: a.n][::-1], a.symbols)
+        assert np.array_equal(outs[2].numpy()[: b.n], b.symbols)
+        assert (outs[0].numpy()[a.n:] == 0xCD).all()
+        # the same table again adds nothing resident
+        srv.submit([serve.request_container(bufs[0], outs[0], tag=9)])
+        assert srv.wait(1)[0].status == 0
+        assert srv.stats()["range_in_use"] == base
