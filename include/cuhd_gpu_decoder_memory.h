@@ -4,6 +4,9 @@
 // tables), sized for the largest geometry the planner may choose for
 // num_units units; the subsequence size and thread count of the reference
 // constructor are accepted and kept, and used as planning hints.
+// reserve() grows the workspace before a decode whose plan captures
+// symbols (the capture slices scale with the output size, which the
+// constructor does not see).
 // get_sync_info() returns the start of the workspace, get_output_sizes()
 // and the sync-flag getters return null: this decoder has no host
 // round-trips and no per-subsequence count array.
@@ -34,6 +37,7 @@ public:
     std::uint8_t* get_sequence_synced_host();
 
     // workspace for the C ABI (mans_decode)
+    void reserve(size_t bytes);
     void* get_workspace() { return workspace_; }
     size_t get_workspace_size() const { return bytes_; }
     size_t get_subsequence_size() const { return subsequence_size_; }

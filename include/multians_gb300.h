@@ -57,6 +57,7 @@ typedef struct {
     uint32_t walk_slots;      /* regions a sync walk may cross */
     uint32_t threads;         /* threads per CTA */
     uint32_t flags;           /* MANS_DECODE_* */
+    uint32_t capture_bytes;   /* symbol capture bytes per region (0: none) */
 } mans_cfg;
 
 /* Output order.  By default the output is in decode order, reversed like
@@ -66,6 +67,16 @@ typedef struct {
  * in order and no host reversal is needed (CUHDOutputBuffer::reverse,
  * src/multians_output_buffer.cc:27-29, fused into the write). */
 #define MANS_DECODE_SOURCE_ORDER 0x1u
+
+/* Symbol capture.  When the stream has at least two bits per symbol on
+ * average (few zero-bit codewords) and L <= 1024, the planner gives every sync
+ * region capture_bytes of workspace: the sync passes, which decode each
+ * region once from a guessed state anyway, keep the symbols they decode
+ * there, and the final pass copies every block whose owning trajectory was
+ * captured instead of decoding it a second time.  MANS_DECODE_NO_CAPTURE
+ * turns this off (smaller workspace, every block decoded in the final
+ * pass); the output is identical either way. */
+#define MANS_DECODE_NO_CAPTURE 0x2u
 
 /* Fills `out` with the geometry the decoder uses for this call. */
 int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,

@@ -16,6 +16,8 @@ from ._lib import (  # noqa: F401
     DEV_SYNC_OVERFLOW,
     DEV_DEGENERATE,
     DEV_COUNT_MISMATCH,
+    DECODE_SOURCE_ORDER,
+    DECODE_NO_CAPTURE,
     lib,
     plan,
     aux_size,

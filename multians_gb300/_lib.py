@@ -38,12 +38,13 @@ class MansError(RuntimeError):
 
 
 DECODE_SOURCE_ORDER = 0x1
+DECODE_NO_CAPTURE = 0x2
 
 
 class Cfg(ctypes.Structure):
     _fields_ = [("block_units", ctypes.c_uint32), ("region_blocks", ctypes.c_uint32),
                 ("walk_slots", ctypes.c_uint32), ("threads", ctypes.c_uint32),
-                ("flags", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32), ("capture_bytes", ctypes.c_uint32)]
 
     def as_dict(self):
         return {f: int(getattr(self, f)) for f, _ in self._fields_}

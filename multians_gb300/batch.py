@@ -39,13 +39,16 @@ def _sig():
 
 
 def desc(units, n_units, out, n_out, table, L, first_state, first_bit,
-         source_order: bool = False) -> StreamDesc:
+         source_order: bool = False, capture: bool = True) -> StreamDesc:
     """A stream descriptor from CUDA tensors (units/table int32 or uint32
-    views); ``source_order`` writes the output in source order."""
+    views); ``source_order`` writes the output in source order, ``capture``
+    False keeps the stream out of symbol capture."""
+    from ._lib import DECODE_NO_CAPTURE, DECODE_SOURCE_ORDER
+    flags = (DECODE_SOURCE_ORDER if source_order else 0) | (0 if capture else DECODE_NO_CAPTURE)
     return StreamDesc(units.data_ptr() if units is not None else None, int(n_units),
                       out.data_ptr() if out is not None else None, int(n_out),
                       table.data_ptr() if table is not None else None, int(L),
-                      int(first_state), int(first_bit), 1 if source_order else 0)
+                      int(first_state), int(first_bit), flags)
 
 
 class Batch:

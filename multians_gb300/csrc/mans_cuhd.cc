@@ -45,6 +45,19 @@ void cuhd::CUHDGPUDecoderMemory::allocate() {
     is_allocated_ = true;
 }
 
+void cuhd::CUHDGPUDecoderMemory::reserve(size_t bytes) {
+    allocate();
+    if (bytes <= bytes_) return;
+    void* grown = nullptr;
+    if (cudaMalloc(&grown, bytes) != cudaSuccess) {
+        cudaGetLastError();   // keep the smaller workspace: the decode runs without capture
+        return;
+    }
+    cudaFree(workspace_);
+    workspace_ = grown;
+    bytes_ = bytes;
+}
+
 void cuhd::CUHDGPUDecoderMemory::free() {
     if (!is_allocated_) return;
     cudaFree(workspace_);
@@ -71,6 +84,9 @@ int cuhd::CUHDGPUDecoder::decode_status(
     size_t /*preferred_subsequence_size*/, size_t /*threads_per_block*/) {
     if (!input || !output || !table || !aux) return MANS_ERR_ARG;
     aux->allocate();
+    mans_cfg plan;
+    if (input_size && mans_plan(input_size, output_size, number_of_states, nullptr, &plan) == MANS_OK)
+        aux->reserve(mans_aux_size(input_size, &plan));
     uint32_t dev_status = 0;
     return mans_decode_sync(input->get(), input_size, output->get(), output_size,
                             reinterpret_cast<const uint32_t*>(table->get()), number_of_states,

@@ -81,6 +81,10 @@ struct DecodeParams {
     uint32_t stage_cap;    // staging bytes per warp in k_final (multiple of 16)
     uint32_t wcap;         // blocks a merge walk may run inside the G pass
     uint32_t flags;        // MANS_DECODE_*
+    uint8_t* cap;          // [nreg * cap_bytes + 16] captured symbols, by region
+    uint32_t* cap_valid;   // [nreg] leading symbols of Gamma_k captured in slice k
+    uint32_t cap_bytes;    // capture bytes per region (0: no capture)
+    uint32_t* fb_list;     // [nblk / 32] warps the copy pass leaves to the decoding pass
 };
 
 // Checks and converts the reference table, then builds both shared-memory
@@ -212,6 +216,56 @@ __device__ __forceinline__ void ring_fill(uint32_t slot_addr, const uint32_t* __
     }
 }
 
+// Symbol capture in the sync passes (DecodeParams::cap_bytes != 0).  A lane
+// keeps the symbols of its trajectory in a ring of 32 words: its column of
+// a warp-wide block of shared memory, row r at byte 128 r, so the 32 lanes
+// of a warp store to 32 different banks whatever their counts.  Symbol c
+// lies in byte c mod 4 of row (c / 4) mod 32.  Each step shifts the symbol
+// into the register word of the last four symbols and stores that word to
+// its row; the row holds the right bytes once its fourth symbol is in.
+// Completed 16-byte groups go to the trajectory's slice of the capture
+// buffer at the start of every round; a lane whose ring wrapped before a
+// flush, or whose count passed the slice, stops capturing, and cap_valid
+// records how many leading symbols of the slice are right.
+constexpr uint32_t kCapRing = 128;                  // symbols a lane's ring holds
+constexpr uint32_t kCapWarpBytes = kCapRing * 32;   // shared bytes per warp
+
+struct CapLane {
+    uint32_t col;    // shared address of the lane's word in row 0
+    uint32_t acc;    // the last four symbols, newest in byte 3
+    uint32_t done;   // leading symbols copied to the slice
+    bool on;         // capture still complete
+};
+
+__device__ __forceinline__ uint32_t cap_row(uint32_t col, uint32_t c) {
+    return col + ((c << 5) & 0xF80u);   // row (c / 4) mod 32
+}
+
+// Copies the completed groups of the first `count` symbols (all of them,
+// the last group padded, when `final`) to dst, at most `limit` bytes
+// (a multiple of 16).
+__device__ __forceinline__ void cap_flush(CapLane& cl, uint8_t* __restrict__ dst,
+                                          uint32_t count, uint32_t limit, bool final) {
+    if (!cl.on) return;
+    if (count - cl.done > kCapRing) {   // the ring wrapped before this flush
+        cl.on = false;
+        return;
+    }
+    if (final && (count & 3u)) sts32(cap_row(cl.col, count), cl.acc >> (8u * (4u - (count & 3u))));
+    uint32_t upto = final ? (count + 15u) & ~15u : count & ~15u;
+    upto = min(upto, limit);
+    for (; cl.done + 16 <= upto; cl.done += 16) {
+        const uint32_t a = cap_row(cl.col, cl.done);
+        uint4 v;
+        v.x = lds32(a);
+        v.y = lds32(a + 128);
+        v.z = lds32(a + 256);
+        v.w = lds32(a + 384);
+        *reinterpret_cast<uint4*>(dst + cl.done) = v;
+    }
+    if (count > limit) cl.on = false;   // the slice is full
+}
+
 // One lane per region k: decode Gamma_k over the region's blocks, record
 // every block's entry (rec_g) and, for k + 1 < nreg, Gamma_k's entry at the
 // first block of region k + 1 (walk slot 0 of that block).  Then the lane
@@ -223,9 +277,11 @@ __device__ __forceinline__ void ring_fill(uint32_t slot_addr, const uint32_t* __
 // (whose successor region belongs to another warp), go to the job list of
 // the merge-walk pass (k_wwalk).
 constexpr uint32_t kWalkCapUnits = 128;
+template <bool kCap>
 __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase) {
     extern __shared__ __align__(16) uint2 s_tab[];
-    load_prepared(s_tab, p.tab_sync, p.L);
+    // capture decodes symbol by symbol; otherwise zero-bit runs are folded
+    load_prepared(s_tab, kCap ? p.tab_sym : p.tab_sync, p.L);
     if (*(volatile uint32_t*) p.status & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE)) return;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t tb = smem_addr(s_tab);
@@ -275,8 +331,15 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
         __syncwarp();
     }
 
-    SCursorLazy A;   // 17+ warps per SM: shared-memory wavefronts bound this pass
+    SCursorLazy A;   // 16+ warps per SM: shared-memory wavefronts bound this pass
     uint32_t ca = 0;
+    CapLane cl;
+    cl.col = ((tb + tab_bytes + blockDim.x * kRingStride + (blockDim.x >> 5) * 40 + 15) & ~15u) +
+             warp * kCapWarpBytes + lane * 4;
+    cl.acc = 0;
+    cl.done = 0;
+    cl.on = kCap;
+    uint8_t* const cdst = kCap ? p.cap + (size_t) k * p.cap_bytes : nullptr;
     uint32_t b = b0;        // block being decoded
     uint32_t bs = 0;        // relative start bit of the current half block
     uint32_t half = 0;      // 0: first half of block b, 1: second half
@@ -286,13 +349,18 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
     if (active) {
         A.init(rs, origin, start, tb + 8u * p.first_idx);
         p.rec_g[b0] = make_rec(A.pos, entry_index(A.a, tb), 0);
-        if (b0 == b1) active = false;
+        if (b0 == b1) {
+            active = false;
+            if (kCap) p.cap_valid[k] = 0;
+        }
     }
 
     const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
     uint32_t r = 0;
     while (__any_sync(0xffffffffu, active)) {
         __syncwarp();   // orders the records of earlier rounds for the other lanes
+        const bool was_active = active;
+        if (kCap && active) cap_flush(cl, cdst, ca, p.cap_bytes, false);
         // refill: wait for round r-2's copies, then issue this round's
         if (r >= 2 && !mbar_wait(bars + 8 * ((r - 2) & 3), ((r - 2) >> 2) & 1)) {
             timed_out = true;
@@ -329,7 +397,17 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
         if (active) {
             // decode to the end of the half block
             const uint32_t be = bs + Hbits;
-            while (A.pos < be) ca += A.step(rs) >> 24;
+            if (kCap) {
+                uint32_t cs = ca << 5;   // 32 x count: its bits 7..11 pick the ring row
+                while (A.pos < be) {
+                    cl.acc = __byte_perm(cl.acc, A.step(rs), 0x7321);
+                    sts32(cl.col + (cs & 0xF80u), cl.acc);
+                    cs += 32;
+                }
+                ca = cs >> 5;
+            } else {
+                while (A.pos < be) ca += A.step(rs) >> 24;
+            }
             bs = be;
             half ^= 1u;
             if (half == 0) {
@@ -368,6 +446,12 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
                 }
             }
         }
+        if (kCap && was_active && !active) {
+            // the trajectory ends here (merged, at the stream end, or handed
+            // to the merge-walk pass, which does not capture)
+            cap_flush(cl, cdst, ca, p.cap_bytes, true);
+            p.cap_valid[k] = cl.on ? ca : cl.done;
+        }
     }
     // drain: no copy may still be writing this CTA's shared memory at exit
     for (uint32_t q = (r >= 2 ? r - 2 : 0); q < r; ++q) {
@@ -379,8 +463,9 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
     if (timed_out) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
 }
 
+template <bool kCap>
 __global__ void __launch_bounds__(kSyncThreadsMax) k_gwalk(DecodeParams p) {
-    gwalk_body(p, blockIdx.x * blockDim.x);
+    gwalk_body<kCap>(p, blockIdx.x * blockDim.x);
 }
 
 // Sync stage, merge walks (k_wwalk): region k's walk continues Gamma_k from
@@ -407,19 +492,25 @@ __global__ void __launch_bounds__(kSyncThreadsMax) k_gwalk(DecodeParams p) {
 // region start it resumes from Gamma_j's entry there (walk slot 0, from the
 // G pass).  Once both cursors follow Gamma_j their entries coincide, which
 // is the merge.
+// With capture, a walk that the G pass handed over while its capture was
+// complete (cap_valid == its count) keeps capturing Gamma_k through region
+// k + 1, where Gamma_k owns the blocks before its merge: in the lane's ring
+// of capture words as in the G pass, flushed every half block, after the
+// ring is primed with the partial group the G pass wrote.
 constexpr uint32_t kWalkThreads = 64;
 constexpr uint32_t kWalkCtasMax = 152 * 8;
 constexpr uint32_t kWindowUnits = 128;
 constexpr uint32_t kWindowTile = (kWindowUnits + 4) * 4;     // bytes per lane
 constexpr uint32_t kWindowStride = kWindowTile;   // 132 words: 8 bank groups, 16-byte aligned
 
+template <bool kCap>
 __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
     extern __shared__ __align__(16) uint2 s_tab[];
     const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
     uint32_t* const job_next = p.scan_flags + ntile + 2;   // next job to take
     const uint32_t njobs = *(volatile uint32_t*) (p.scan_flags + ntile + 1);
     if (njobs == 0 || *(volatile uint32_t*) job_next >= njobs) return;   // nothing left
-    load_prepared(s_tab, p.tab_sync, p.L);
+    load_prepared(s_tab, kCap ? p.tab_sym : p.tab_sync, p.L);
     if (*(volatile uint32_t*) p.status & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE)) return;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t tb = smem_addr(s_tab);
@@ -444,6 +535,13 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
     // count while following); G likewise (g_rec = ~0: not a cursor yet)
     uint32_t jk = 0, jb = 0, a_rec = 0, ca = 0, g_rec = ~0u, cg = 0, fl = 0;
     bool timed_out = false;
+    CapLane cl;
+    cl.col = ((tb + tab_bytes + blockDim.x * kWindowStride + (blockDim.x >> 5) * 8 + 15) & ~15u) +
+             warp * kCapWarpBytes + lane * 4;
+    cl.acc = 0;
+    cl.done = 0;
+    cl.on = false;
+    uint8_t* slice = nullptr;
     for (uint32_t win = 0;; ++win) {
         // lanes without a walk take the next jobs
         const uint32_t need = __ballot_sync(0xffffffffu, !open);
@@ -460,6 +558,25 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
                     jk = v0.x; jb = v0.y; a_rec = v0.z; ca = v0.w;
                     g_rec = v1.x; cg = v1.y; fl = v1.z;
                     open = true;
+                    if (kCap) {
+                        // capture goes on where the G pass's was complete
+                        slice = p.cap + (size_t) jk * p.cap_bytes;
+                        cl.on = !(fl & kAFollow) && jb / p.nb == jk + 1 &&
+                                __ldcg(p.cap_valid + jk) == ca;
+                        if (cl.on) {
+                            // the open group's bytes below ca, as the G pass wrote them
+                            const uint32_t g0 = ca & ~15u;
+                            const uint4 g = *reinterpret_cast<const uint4*>(slice + g0);
+                            sts32(cap_row(cl.col, g0), g.x);
+                            sts32(cap_row(cl.col, g0 + 4), g.y);
+                            sts32(cap_row(cl.col, g0 + 8), g.z);
+                            sts32(cap_row(cl.col, g0 + 12), g.w);
+                            const uint32_t wi = (ca >> 2) & 3u, j = ca & 3u;
+                            const uint32_t part = wi == 0 ? g.x : (wi == 1 ? g.y : (wi == 2 ? g.z : g.w));
+                            cl.acc = j ? part << (8u * (4u - j)) : 0u;
+                            cl.done = g0;
+                        }
+                    }
                 }
             }
         }
@@ -551,14 +668,47 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
             // walk block b with the cursors that do not follow
             const uint32_t be = bs + Bbits;
             const bool sa = !(fl & kAFollow), sg = d >= 2 && !(fl & kGFollow);
-            if (sa && sg) {
-                while (A.pos < be && G.pos < be) {
-                    ca += A.step(src) >> 24;
-                    cg += G.step(src) >> 24;
+            if (kCap) {
+                // symbol table: one symbol per step; only A (at d == 1) captures
+                if (sa && sg) {
+                    while (A.pos < be && G.pos < be) {
+                        A.step(src);
+                        ++ca;
+                        G.step(src);
+                        ++cg;
+                    }
                 }
+                if (sa && cl.on) {
+                    // d == 1: capture, flushing at the half block and the block end
+                    uint32_t cs = ca << 5;
+                    const uint32_t mid = bs + (Bbits >> 1);
+                    while (A.pos < mid) {
+                        cl.acc = __byte_perm(cl.acc, A.step(src), 0x7321);
+                        sts32(cl.col + (cs & 0xF80u), cl.acc);
+                        cs += 32;
+                    }
+                    cap_flush(cl, slice, cs >> 5, p.cap_bytes, false);
+                    while (A.pos < be) {
+                        cl.acc = __byte_perm(cl.acc, A.step(src), 0x7321);
+                        sts32(cl.col + (cs & 0xF80u), cl.acc);
+                        cs += 32;
+                    }
+                    ca = cs >> 5;
+                    cap_flush(cl, slice, ca, p.cap_bytes, false);
+                    if (!cl.on) p.cap_valid[jk] = cl.done;   // the capture broke off
+                }
+                if (sa) while (A.pos < be) { A.step(src); ++ca; }
+                if (sg) while (G.pos < be) { G.step(src); ++cg; }
+            } else {
+                if (sa && sg) {
+                    while (A.pos < be && G.pos < be) {
+                        ca += A.step(src) >> 24;
+                        cg += G.step(src) >> 24;
+                    }
+                }
+                if (sa) while (A.pos < be) ca += A.step(src) >> 24;
+                if (sg) while (G.pos < be) cg += G.step(src) >> 24;
             }
-            if (sa) while (A.pos < be) ca += A.step(src) >> 24;
-            if (sg) while (G.pos < be) cg += G.step(src) >> 24;
             bs = be;
             jb = b + 1;
             rg = rg_next;
@@ -568,6 +718,17 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
                 p.delta[jk] = 0;
                 open = false;
             }
+            // the capture covers region k + 1 only
+            if (kCap && cl.on && (!open || reg != jk + 1)) {
+                cap_flush(cl, slice, ca, p.cap_bytes, true);
+                p.cap_valid[jk] = cl.on ? ca : cl.done;
+                cl.on = false;
+            }
+        }
+        if (kCap && cl.on && !open) {   // merged, or out of slots
+            cap_flush(cl, slice, ca, p.cap_bytes, true);
+            p.cap_valid[jk] = cl.on ? ca : cl.done;
+            cl.on = false;
         }
         if (open) {
             if (!(fl & kAFollow)) a_rec = (A.pos - bs) | (entry_index(A.a, tb) << 8);
@@ -577,7 +738,8 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
     if (timed_out) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
 }
 
-__global__ void __launch_bounds__(kWalkThreads) k_wwalk(DecodeParams p) { wwalk_body(p); }
+template <bool kCap>
+__global__ void __launch_bounds__(kWalkThreads) k_wwalk(DecodeParams p) { wwalk_body<kCap>(p); }
 
 // Tiles are taken in launch order through an atomic ticket (the word after
 // the flags), so a tile only waits on tiles that have already started.
@@ -588,60 +750,154 @@ __global__ void __launch_bounds__(kScanThreads) k_scan(DecodeParams p) {
     scan_body(p, s_tile);
 }
 
-// Entry (bit offset from the block start, state index) and global output
-// offset of block b.  Returns false when no trajectory owns the block (a
-// walk ran out of slots).
-__device__ __forceinline__ bool block_entry(const DecodeParams& p, uint32_t b,
-                                            uint32_t& rel, uint32_t& idx,
-                                            unsigned long long& off) {
+__device__ __forceinline__ void sts8(uint32_t a, uint32_t v) {
+    asm volatile("st.shared.u8 [%0], %1;" :: "r"(a), "r"(v) : "memory");
+}
+
+// Owner of block b: d = region(b) - k for the owning trajectory Gamma_k, its
+// record at b and its output offset there.  Returns false when no
+// trajectory owns the block (a walk ran out of slots).
+__device__ __forceinline__ bool block_owner(const DecodeParams& p, uint32_t b, uint32_t& d,
+                                            uint2& rec, unsigned long long& off) {
     const uint64_t bs = (uint64_t) b * p.B * 32;
     const uint32_t r = b / p.nb;
-    uint32_t d = 0;
-    for (;; ++d) {
+    for (d = 0;; ++d) {
         if (d > r || d > p.dmax) return false;
         if (p.Mpre[r - d] <= bs) break;
     }
-    const uint2 rec = d == 0 ? p.rec_g[b] : p.rec_w[(size_t) b * p.dmax + (d - 1)];
+    rec = d == 0 ? p.rec_g[b] : p.rec_w[(size_t) b * p.dmax + (d - 1)];
     off = (unsigned long long) (p.Dpre[r - d] + (long long) rec.y);
+    return true;
+}
+
+// Entry (bit offset from the block start, state index) and global output
+// offset of block b.
+__device__ __forceinline__ bool block_entry(const DecodeParams& p, uint32_t b,
+                                            uint32_t& rel, uint32_t& idx,
+                                            unsigned long long& off) {
+    uint32_t d;
+    uint2 rec;
+    if (!block_owner(p, b, d, rec, off)) return false;
     idx = min(rec.x >> 8, p.L - 1);   // records come from the sync stage; the clamp keeps
     rel = rec.x & 0xffu;              // table addresses in range regardless
     return true;
 }
 
-// One warp per 32 consecutive blocks, one lane per block.  Each lane's
-// input (its block plus four units of look-ahead) arrives in shared memory
-// by a TMA bulk copy into a lane-private tile; the tiles sit kTileStride
-// bytes apart so lanes reading the same relative unit spread over eight
-// bank groups.  The symbol count of every block is known from the scan, so
-// a lane decodes exactly that many symbols (and checks that it ended at
-// the next block start).  The 32 blocks' symbols form one contiguous output
-// range; lanes decode into a shared staging buffer laid out with the same
-// 16-byte phase as the output, then the warp writes the range with 16-byte
-// stores (bytes at the unaligned ends).  A range larger than the staging
-// buffer is written byte by byte instead.
-constexpr uint32_t kFinalThreads = 256;   // eight warps share one table copy
-
-__device__ __forceinline__ void sts8(uint32_t a, uint32_t v) {
-    asm volatile("st.shared.u8 [%0], %1;" :: "r"(a), "r"(v) : "memory");
+__device__ __forceinline__ void sts128(uint32_t a, uint4 v) {
+    asm volatile("st.shared.v4.u32 [%0], {%1, %2, %3, %4};"
+                 :: "r"(a), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
 }
 
+// Copies len captured bytes into the staging buffer: staging byte t0 + j
+// gets cap[s0 + j], or with kRev cap[s0 + len - 1 - j].  Single bytes up to
+// the first 16-byte staging boundary and after the last; in between every
+// lane takes 16-byte chunks, four at a time (their 20 source words in
+// flight together: the copy is bound by load latency otherwise), and
+// assembles each from five aligned source words by funnel shifts.  Source
+// words may extend up to 4 bytes past the range (inside the buffer's pad).
 template <bool kRev>
-__device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, uint32_t nctas) {
+__device__ __forceinline__ void stage_copy(uint32_t t0, const uint8_t* __restrict__ cap,
+                                           unsigned long long s0, uint32_t len, uint32_t lane) {
+    const uint32_t head = min(len, (16u - (t0 & 15u)) & 15u);
+    const uint32_t nc = (len - head) >> 4;
+    const uint32_t tail = (len - head) & 15u;
+    if (lane < head + tail) {
+        const uint32_t j = lane < head ? lane : head + nc * 16 + (lane - head);
+        sts8(t0 + j, cap[kRev ? s0 + len - 1 - j : s0 + j]);
+    }
+    constexpr int kU = 4;
+    for (uint32_t c0 = 0; c0 < nc; c0 += kU * 32) {
+        uint32_t w[kU][5];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t c = c0 + u * 32 + lane;
+            const uint32_t j = head + 16 * c;
+            const unsigned long long e = kRev ? s0 + len - 16 - j : s0 + j;   // lowest source byte
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(cap + (e & ~3ull));
+#pragma unroll
+            for (int i = 0; i < 5; ++i) w[u][i] = c < nc ? __ldg(q + i) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t c = c0 + u * 32 + lane;
+            if (c < nc) {
+                const uint32_t j = head + 16 * c;
+                const unsigned long long e = kRev ? s0 + len - 16 - j : s0 + j;
+                const uint32_t sh = (uint32_t) (e & 3u) * 8u;
+                uint4 v;
+                if (!kRev) {
+                    v.x = __funnelshift_r(w[u][0], w[u][1], sh);
+                    v.y = __funnelshift_r(w[u][1], w[u][2], sh);
+                    v.z = __funnelshift_r(w[u][2], w[u][3], sh);
+                    v.w = __funnelshift_r(w[u][3], w[u][4], sh);
+                } else {
+                    v.x = __byte_perm(__funnelshift_r(w[u][3], w[u][4], sh), 0, 0x0123);
+                    v.y = __byte_perm(__funnelshift_r(w[u][2], w[u][3], sh), 0, 0x0123);
+                    v.z = __byte_perm(__funnelshift_r(w[u][1], w[u][2], sh), 0, 0x0123);
+                    v.w = __byte_perm(__funnelshift_r(w[u][0], w[u][1], sh), 0, 0x0123);
+                }
+                sts128(t0 + j, v);
+            }
+        }
+    }
+}
+
+// One warp per 32 consecutive blocks, one lane per block.  The 32 blocks'
+// symbols form one contiguous output range; lanes fill a shared staging
+// buffer laid out with the same 16-byte phase as the output, then the warp
+// writes the range with 16-byte stores (bytes at the unaligned ends).  A
+// range larger than the staging buffer is written byte by byte instead.
+//
+// A block whose owning trajectory was captured by the sync passes is
+// copied: its symbols are Gamma_r's (r = its region) when the owner's entry
+// equals Gamma_r's record at the block, else the owner's own, and either
+// slice holds them when cap_valid covers the block's count range.  Lanes
+// whose blocks abut in both the capture and the output form segments that
+// the warp copies together.  Every other block is decoded: its input (the
+// block plus four units of look-ahead) arrives in shared memory by a TMA
+// bulk copy into a lane-private tile (tiles kTileStride bytes apart, so
+// lanes reading the same relative unit spread over eight bank groups), and
+// the lane decodes exactly the block's symbol count, known from the scan,
+// checking that it ended at the next block start.
+constexpr uint32_t kFinalThreads = 256;   // eight warps share one table copy
+
+// Shared-memory address of a final-pass warp's mbarrier.
+__device__ __forceinline__ uint32_t final_bar(const DecodeParams& p, uint32_t tb, uint32_t warp) {
+    const uint32_t tile_units = p.B + 4;
+    const uint32_t tile_stride = tile_units * 4 + (((tile_units * 4) & 127) == 0 ? 16 : 0);
+    const uint32_t per_warp = 32 * tile_stride + 16 + p.stage_cap + 16;
+    const uint32_t tab_bytes = (p.L * 8 + 15) & ~15u;
+    return tb + tab_bytes + warp * per_warp + 32 * tile_stride;
+}
+
+// CTA prologue of the final passes: the symbol table into shared memory;
+// a single-symbol table fills the output (when `fill`).  Returns false when
+// the CTA has nothing more to do.
+__device__ __forceinline__ bool final_prologue(const DecodeParams& p, uint32_t cta,
+                                               uint32_t nctas, bool fill) {
     extern __shared__ __align__(16) uint2 s_tab[];
     load_prepared(s_tab, p.tab_sym, p.L);
     const uint32_t st = *(volatile uint32_t*) p.status;
     if (st & MANS_DEV_DEGENERATE) {
         // single-symbol table: every state decodes that symbol
+        if (!fill) return false;
         const uint8_t sym = (uint8_t) (__ldg(p.table) >> 16);
         const unsigned long long stride = (unsigned long long) nctas * blockDim.x;
         for (unsigned long long i = (unsigned long long) cta * blockDim.x + threadIdx.x;
              i < p.n_out; i += stride)
             p.out[i] = sym;
-        return;
+        return false;
     }
-    if (st & (MANS_DEV_BAD_TABLE | MANS_DEV_SYNC_OVERFLOW | MANS_DEV_SCAN_TIMEOUT)) return;
+    return !(st & (MANS_DEV_BAD_TABLE | MANS_DEV_SYNC_OVERFLOW | MANS_DEV_SCAN_TIMEOUT));
+}
 
-    const uint32_t tb = smem_addr(s_tab);
+// The final pass for the warp of blocks b0 .. b0 + 31 (its mbarrier
+// initialised, expecting parity `phase`).  Returns false after an error
+// (reported in the status word).
+template <bool kRev>
+__device__ __forceinline__ bool final_warp(const DecodeParams& p, uint32_t tb, uint32_t b0,
+                                           uint32_t phase) {
+    extern __shared__ __align__(16) uint2 s_tab[];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t tile_units = p.B + 4;                 // 16-byte multiple (B % 4 == 0)
     const uint32_t tile_stride = tile_units * 4 + (((tile_units * 4) & 127) == 0 ? 16 : 0);
@@ -652,35 +908,13 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
     const uint32_t bar = wbase + 32 * tile_stride;       // 16 bytes reserved
     const uint32_t stage_addr = bar + 16;
 
-    const uint32_t b0 = cta * blockDim.x + (warp << 5);
-    if (b0 >= p.nblk) return;
     const uint32_t b = b0 + lane;
     const bool have = b < p.nblk;
 
-    // stage the lane tiles
-    const uint32_t* __restrict__ in = p.units;
-    const uint32_t n = p.n_units;
-    const uint32_t u0 = b * p.B;
-    if (lane == 0) {
-        mbar_init(bar, 1);
-        fence_mbar_init();
-    }
-    __syncwarp();
-    const uint32_t avail_units = (have && u0 < n) ? min(tile_units, n - u0) : 0u;
-    const uint32_t bulk_units = avail_units & ~3u;
-    const uint32_t total = __reduce_add_sync(0xffffffffu, bulk_units * 4);
-    if (lane == 0) mbar_arrive_expect_tx(bar, total);
-    __syncwarp();
-    if (bulk_units) {
-        fence_proxy_async();
-        tma_load(tile, in + u0, bulk_units * 4, bar);
-    }
-    for (uint32_t i = bulk_units; i < tile_units; ++i)
-        sts32(tile + i * 4, i < avail_units ? __ldg(in + u0 + i) : 0u);
-
-    uint32_t rel = 0, idx = 0;
+    uint32_t d = 0;
+    uint2 rec = make_uint2(0, 0);
     unsigned long long off = 0;
-    bool ok = have ? block_entry(p, b, rel, idx, off) : true;
+    bool ok = have ? block_owner(p, b, d, rec, off) : true;
     // offset of block b + 1; the last block runs to the end of the output
     // (writes stop at n_out), which may lie before or after its start
     unsigned long long off_nx = max((unsigned long long) p.n_out, off);
@@ -690,12 +924,10 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
         uint32_t tr, ti;
         ok &= block_entry(p, b + 1, tr, ti, off_nx);
     }
-    bool staged_in = mbar_wait(bar, 0);
-    if (!staged_in) mbar_wait(bar, 0);   // never exit with the copy in flight
     __syncwarp();
-    if (__any_sync(0xffffffffu, !ok || !staged_in)) {
-        if (lane == 0) atomicOr(p.status, staged_in ? MANS_DEV_SYNC_OVERFLOW : MANS_DEV_SCAN_TIMEOUT);
-        return;
+    if (__any_sync(0xffffffffu, !ok)) {
+        if (lane == 0) atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
+        return false;
     }
     const unsigned long long off0 = __shfl_sync(0xffffffffu, off, 0);
     const uint32_t last_lane = min(31u, p.nblk - 1 - b0);
@@ -716,22 +948,65 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
     const bool lane_ok = !have || (off >= off0 && max(off_nx, off) <= max(off_end, off0));
     if (__any_sync(0xffffffffu, !lane_ok)) {
         if (lane == 0) atomicOr(p.status, MANS_DEV_COUNT_MISMATCH);
-        return;
+        return false;
     }
-    if (have) {
-        // symbols of this block that land in [.., n_out)
-        const unsigned long long end = min(max(off_nx, off), p.n_out);
-        // a valid block holds at most (B * 32 + 17) bit positions, each with
-        // fewer than L codewords: the cap keeps a corrupted offset from
-        // running the loop (or its tile reads) away
-        const unsigned long long cap_sym = (unsigned long long) (p.B * 32 + 17) * p.L;
-        const uint32_t cnt = off < end ? (uint32_t) min(end - off, cap_sym) : 0u;
+    // symbols of this block that land in [.., n_out)
+    const unsigned long long end = min(max(off_nx, off), p.n_out);
+    // a valid block holds at most (B * 32 + 17) bit positions, each with
+    // fewer than L codewords: the cap keeps a corrupted offset from
+    // running the loop (or its tile reads) away
+    const unsigned long long cap_sym = (unsigned long long) (p.B * 32 + 17) * p.L;
+    const uint32_t cnt = have && off < end ? (uint32_t) min(end - off, cap_sym) : 0u;
+
+    // captured blocks: slice ck from count cy
+    bool capd = false;
+    unsigned long long csrc = 0;
+    if (p.cap_bytes && staged && cnt) {
+        const uint32_t r = b / p.nb;
+        uint32_t ck = r - d, cy = rec.y;
+        if (d > 0) {
+            const uint2 g = __ldg(p.rec_g + b);
+            if (g.x == rec.x) {   // the owner runs on Gamma_r's trajectory here
+                ck = r;
+                cy = g.y;
+            }
+        }
+        capd = (unsigned long long) cy + cnt <= __ldg(p.cap_valid + ck);
+        csrc = (unsigned long long) ck * p.cap_bytes + cy;
+    }
+    const bool dec = have && !capd;
+
+    // stage the tiles of the lanes that decode
+    const uint32_t* __restrict__ in = p.units;
+    const uint32_t n = p.n_units;
+    const uint32_t u0 = b * p.B;
+    const uint32_t avail_units = (dec && u0 < n) ? min(tile_units, n - u0) : 0u;
+    const uint32_t bulk_units = avail_units & ~3u;
+    const uint32_t total = __reduce_add_sync(0xffffffffu, bulk_units * 4);
+    if (lane == 0) mbar_arrive_expect_tx(bar, total);
+    __syncwarp();
+    if (bulk_units) {
+        fence_proxy_async();
+        tma_load(tile, in + u0, bulk_units * 4, bar);
+    }
+    if (dec)
+        for (uint32_t i = bulk_units; i < tile_units; ++i)
+            sts32(tile + i * 4, i < avail_units ? __ldg(in + u0 + i) : 0u);
+    bool staged_in = mbar_wait(bar, phase);
+    if (!staged_in) mbar_wait(bar, phase);   // never exit with the copy in flight
+    __syncwarp();
+    if (__any_sync(0xffffffffu, !staged_in)) {
+        if (lane == 0) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
+        return false;
+    }
+
+    if (dec) {
         const uint32_t pos_cap = p.B * 32 + kMaxBits + 1;
         const uint32_t full = off_nx >= off ? (uint32_t) min(off_nx - off, 0xffffffffull) : 0u;
         SCursorLazy c;
         const UnitSrc ts{tile, u0, ~0u, tile_units - 1};
         const uint64_t bs = (uint64_t) b * p.B * 32;   // cursor units are global indices
-        c.init(ts, bs, bs + rel, tb + 8u * idx);
+        c.init(ts, bs, bs + (rec.x & 0xffu), tb + 8u * min(rec.x >> 8, p.L - 1));
         if (staged && !kRev) {
             // bytes up to a word boundary, then four symbols per 32-bit
             // store, then the remaining bytes
@@ -779,7 +1054,28 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
             (c.pos < p.B * 32 || c.pos >= p.B * 32 + kMaxBits + 1))
             atomicOr(p.status, MANS_DEV_COUNT_MISMATCH);
     }
-    if (!staged || wlo >= whi) return;
+    if (!staged || wlo >= whi) return true;
+    if (p.cap_bytes) {
+        // captured segments: runs of lanes whose capture and output ranges abut
+        __syncwarp();
+        const unsigned long long s_end = csrc + cnt, o_end = off + cnt;
+        const unsigned long long ps = __shfl_up_sync(0xffffffffu, s_end, 1);
+        const unsigned long long po = __shfl_up_sync(0xffffffffu, o_end, 1);
+        const int pc = __shfl_up_sync(0xffffffffu, (int) capd, 1);
+        const bool cont = lane > 0 && capd && pc && ps == csrc && po == off;
+        const uint32_t starts = __ballot_sync(0xffffffffu, capd && !cont);
+        const uint32_t conts = __ballot_sync(0xffffffffu, cont);
+        for (uint32_t rest = starts; rest; rest &= rest - 1) {
+            const uint32_t s0 = __ffs(rest) - 1;
+            const uint32_t after = ~conts & (0xfffffffeu << s0);   // lanes past s0 that start anew
+            const uint32_t e = after ? __ffs(after) - 2 : 31u;     // last lane of the segment
+            const unsigned long long src0 = __shfl_sync(0xffffffffu, csrc, s0);
+            const unsigned long long o0 = __shfl_sync(0xffffffffu, off, s0);
+            const unsigned long long o1 = __shfl_sync(0xffffffffu, o_end, e);
+            const uint32_t t0 = stage_addr + sb + (uint32_t) (kRev ? p.n_out - o1 - wlo : o0 - wlo);
+            stage_copy<kRev>(t0, p.cap, src0, (uint32_t) (o1 - o0), lane);
+        }
+    }
     __syncwarp();
     // [wlo, whi) from stage[sb + (j - wlo)]; aligned middle in 16 B words
     const uint8_t* stage = reinterpret_cast<const uint8_t*>(s_tab) + (stage_addr - tb);
@@ -795,6 +1091,215 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
     uint4* dst = reinterpret_cast<uint4*>(p.out + a0);
     const uint32_t nvec = (uint32_t) ((a1 - a0) >> 4);
     for (uint32_t v = lane; v < nvec; v += 32) dst[v] = src[v];
+    return true;
+}
+
+template <bool kRev>
+__device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, uint32_t nctas) {
+    extern __shared__ __align__(16) uint2 s_tab[];
+    if (!final_prologue(p, cta, nctas, true)) return;
+    const uint32_t tb = smem_addr(s_tab);
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t b0 = cta * blockDim.x + (warp << 5);
+    if (b0 >= p.nblk) return;
+    if ((threadIdx.x & 31) == 0) {
+        mbar_init(final_bar(p, tb, warp), 1);
+        fence_mbar_init();
+    }
+    final_warp<kRev>(p, tb, b0, 0);
+}
+
+// Final pass with capture, first kernel (k_copy): warps whose 32 blocks
+// were all captured copy the symbols straight from the capture slices to
+// the output; every other warp is listed for the decoding kernel
+// (k_final_fb, the final pass above run over the listed warps).  No shared
+// memory, so many warps per SM keep their loads in flight: a warp is a
+// short chain of global loads (owners and records, issued together for
+// walk depths up to 2, then the symbols) and 16-byte stores.
+constexpr uint32_t kCopyThreads = 256;
+
+struct CopyEntry {
+    unsigned long long off;   // output offset of the block's first symbol
+    unsigned long long src;   // capture byte of that symbol
+    uint32_t cy;              // its count in the slice
+    uint32_t valid;           // the slice's captured count
+    bool ok;                  // owner at walk depth <= 2
+};
+
+__device__ __forceinline__ CopyEntry copy_entry(const DecodeParams& p, uint32_t b) {
+    CopyEntry e;
+    e.off = e.src = 0;
+    e.cy = e.valid = 0;
+    e.ok = false;
+    const uint64_t bs = (uint64_t) b * p.B * 32;
+    const uint32_t r = b / p.nb;
+    const uint32_t r1 = r >= 1 ? r - 1 : r, r2 = r >= 2 ? r - 2 : r;
+    const unsigned long long M0 = __ldg(p.Mpre + r), M1 = __ldg(p.Mpre + r1),
+                             M2 = __ldg(p.Mpre + r2);
+    const long long D0 = __ldg(p.Dpre + r), D1 = __ldg(p.Dpre + r1), D2 = __ldg(p.Dpre + r2);
+    const uint32_t V0 = __ldg(p.cap_valid + r), V1 = __ldg(p.cap_valid + r1),
+                   V2 = __ldg(p.cap_valid + r2);
+    const uint2 g = __ldg(p.rec_g + b);
+    uint32_t d;
+    if (M0 <= bs) d = 0;
+    else if (r >= 1 && M1 <= bs) d = 1;
+    else if (r >= 2 && p.dmax >= 2 && M2 <= bs) d = 2;
+    else return e;   // a deeper owner (or none): left to the decoding kernel
+    const uint2 rec = d == 0 ? g : __ldg(p.rec_w + (size_t) b * p.dmax + (d - 1));
+    e.off = (unsigned long long) ((d == 0 ? D0 : (d == 1 ? D1 : D2)) + (long long) rec.y);
+    const bool own = d == 0 || rec.x == g.x;   // on Gamma_r's trajectory here
+    e.cy = own ? g.y : rec.y;
+    e.valid = own ? V0 : (d == 1 ? V1 : V2);
+    e.src = (unsigned long long) (own ? r : r - d) * p.cap_bytes + e.cy;
+    e.ok = true;
+    return e;
+}
+
+// Decode indices [o0, o1) from cap[src0 ..] to the output (index i, or
+// n_out - 1 - i with kRev): single bytes up to the first 16-byte output
+// boundary and after the last, 16-byte stores in between, each assembled
+// from five aligned source words (four chunks per lane in flight).
+template <bool kRev>
+__device__ __forceinline__ void out_copy(uint8_t* __restrict__ out, unsigned long long n_out,
+                                         unsigned long long o0, unsigned long long o1,
+                                         const uint8_t* __restrict__ cap,
+                                         unsigned long long src0, uint32_t lane) {
+    const unsigned long long y0 = kRev ? n_out - o1 : o0;
+    const uint32_t len = (uint32_t) (o1 - o0);
+    const uint32_t head = min(len, (uint32_t) ((16u - (((uintptr_t) out + y0) & 15u)) & 15u));
+    const uint32_t nc = (len - head) >> 4;
+    const uint32_t tail = (len - head) & 15u;
+    if (lane < head + tail) {
+        const uint32_t j = lane < head ? lane : head + nc * 16 + (lane - head);
+        out[y0 + j] = cap[kRev ? src0 + len - 1 - j : src0 + j];
+    }
+    constexpr int kU = 4;
+    for (uint32_t c0 = 0; c0 < nc; c0 += kU * 32) {
+        uint32_t w[kU][5];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t c = c0 + u * 32 + lane;
+            const uint32_t j = head + 16 * c;
+            const unsigned long long e = kRev ? src0 + len - 16 - j : src0 + j;
+            const uint32_t* q = reinterpret_cast<const uint32_t*>(cap + (e & ~3ull));
+#pragma unroll
+            for (int i = 0; i < 5; ++i) w[u][i] = c < nc ? __ldg(q + i) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const uint32_t c = c0 + u * 32 + lane;
+            if (c < nc) {
+                const uint32_t j = head + 16 * c;
+                const unsigned long long e = kRev ? src0 + len - 16 - j : src0 + j;
+                const uint32_t sh = (uint32_t) (e & 3u) * 8u;
+                uint4 v;
+                if (!kRev) {
+                    v.x = __funnelshift_r(w[u][0], w[u][1], sh);
+                    v.y = __funnelshift_r(w[u][1], w[u][2], sh);
+                    v.z = __funnelshift_r(w[u][2], w[u][3], sh);
+                    v.w = __funnelshift_r(w[u][3], w[u][4], sh);
+                } else {
+                    v.x = __byte_perm(__funnelshift_r(w[u][3], w[u][4], sh), 0, 0x0123);
+                    v.y = __byte_perm(__funnelshift_r(w[u][2], w[u][3], sh), 0, 0x0123);
+                    v.z = __byte_perm(__funnelshift_r(w[u][1], w[u][2], sh), 0, 0x0123);
+                    v.w = __byte_perm(__funnelshift_r(w[u][0], w[u][1], sh), 0, 0x0123);
+                }
+                __stcs(reinterpret_cast<uint4*>(out + y0 + j), v);
+            }
+        }
+    }
+}
+
+template <bool kRev>
+__device__ __forceinline__ void copy_body(const DecodeParams& p, uint32_t cta, uint32_t nctas) {
+    const uint32_t st = *(volatile uint32_t*) p.status;
+    if (st & MANS_DEV_DEGENERATE) {
+        const uint8_t sym = (uint8_t) (__ldg(p.table) >> 16);
+        const unsigned long long stride = (unsigned long long) nctas * blockDim.x;
+        for (unsigned long long i = (unsigned long long) cta * blockDim.x + threadIdx.x;
+             i < p.n_out; i += stride)
+            p.out[i] = sym;
+        return;
+    }
+    if (st & (MANS_DEV_BAD_TABLE | MANS_DEV_SYNC_OVERFLOW | MANS_DEV_SCAN_TIMEOUT)) return;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t b0 = cta * blockDim.x + (threadIdx.x & ~31u);
+    if (b0 >= p.nblk) return;
+    const uint32_t b = b0 + lane;
+    const bool have = b < p.nblk;
+    CopyEntry e = have ? copy_entry(p, b) : CopyEntry{0, 0, 0, 0, true};
+    // the next block's offset (lane 31: the first block of the next warp)
+    CopyEntry en{0, 0, 0, 0, true};
+    if (lane == 31 && b + 1 < p.nblk) en = copy_entry(p, b + 1);
+    unsigned long long off_nx = max((unsigned long long) p.n_out, e.off);
+    const unsigned long long from_next = __shfl_down_sync(0xffffffffu, e.off, 1);
+    if (b + 1 < p.nblk) off_nx = lane < 31 ? from_next : en.off;
+    const unsigned long long off0 = __shfl_sync(0xffffffffu, e.off, 0);
+    const uint32_t last_lane = min(31u, p.nblk - 1 - b0);
+    const unsigned long long off_end = __shfl_sync(0xffffffffu, off_nx, last_lane);
+    const bool lane_ok = !have || (e.off >= off0 && max(off_nx, e.off) <= max(off_end, off0));
+    const unsigned long long end = min(max(off_nx, e.off), p.n_out);
+    const uint32_t cnt = have && e.off < end ? (uint32_t) min(end - e.off, 0xffffffffull) : 0u;
+    const bool capd = cnt == 0 || (unsigned long long) e.cy + cnt <= e.valid;
+    if (__any_sync(0xffffffffu, !e.ok || !en.ok || !lane_ok || !capd)) {
+        if (lane == 0) {
+            const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
+            p.fb_list[atomicAdd(p.scan_flags + ntile + 3, 1u)] = b0 >> 5;
+        }
+        return;
+    }
+    // runs of lanes whose capture and output ranges abut: one copy each
+    const bool cp = cnt > 0;
+    const unsigned long long s_end = e.src + cnt, o_end = e.off + cnt;
+    const unsigned long long ps = __shfl_up_sync(0xffffffffu, s_end, 1);
+    const unsigned long long po = __shfl_up_sync(0xffffffffu, o_end, 1);
+    const int pc = __shfl_up_sync(0xffffffffu, (int) cp, 1);
+    const bool cont = lane > 0 && cp && pc && ps == e.src && po == e.off;
+    const uint32_t starts = __ballot_sync(0xffffffffu, cp && !cont);
+    const uint32_t conts = __ballot_sync(0xffffffffu, cont);
+    for (uint32_t rest = starts; rest; rest &= rest - 1) {
+        const uint32_t s0 = __ffs(rest) - 1;
+        const uint32_t after = ~conts & (0xfffffffeu << s0);
+        const uint32_t last = after ? __ffs(after) - 2 : 31u;
+        const unsigned long long src0 = __shfl_sync(0xffffffffu, e.src, s0);
+        const unsigned long long o0 = __shfl_sync(0xffffffffu, e.off, s0);
+        const unsigned long long o1 = __shfl_sync(0xffffffffu, o_end, last);
+        out_copy<kRev>(p.out, p.n_out, o0, o1, p.cap, src0, lane);
+    }
+}
+
+template <bool kRev>
+__global__ void __launch_bounds__(kCopyThreads) k_copy(DecodeParams p) {
+    copy_body<kRev>(p, blockIdx.x, gridDim.x);
+}
+
+// The decoding final pass over the warps k_copy listed (persistent grid).
+template <bool kRev>
+__device__ __forceinline__ void final_fb_body(const DecodeParams& p, uint32_t cta,
+                                              uint32_t nctas) {
+    extern __shared__ __align__(16) uint2 s_tab[];
+    const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
+    const uint32_t count = *(volatile uint32_t*) (p.scan_flags + ntile + 3);
+    const uint32_t wpc = blockDim.x >> 5;
+    if (cta * wpc >= count) return;   // the whole CTA is idle
+    if (!final_prologue(p, cta, nctas, false)) return;
+    const uint32_t tb = smem_addr(s_tab);
+    const uint32_t warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        mbar_init(final_bar(p, tb, warp), 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    uint32_t phase = 0;
+    for (uint32_t i = cta * wpc + warp; i < count; i += nctas * wpc) {
+        if (!final_warp<kRev>(p, tb, p.fb_list[i] << 5, phase)) return;
+        phase ^= 1u;
+    }
+}
+
+template <bool kRev>
+__global__ void __launch_bounds__(kFinalThreads) k_final_fb(DecodeParams p) {
+    final_fb_body<kRev>(p, blockIdx.x, gridDim.x);
 }
 
 template <bool kRev>
@@ -834,7 +1339,8 @@ __global__ void __launch_bounds__(kSyncThreads) k_gwalk_batch(const DecodeParams
     __shared__ DecodeParams sp;
     const BatchItem it = items[blockIdx.x];
     load_params(sp, ps + it.stream);
-    gwalk_body(sp, it.index);
+    if (sp.cap_bytes) gwalk_body<true>(sp, it.index);
+    else gwalk_body<false>(sp, it.index);
 }
 
 __global__ void __launch_bounds__(kWalkThreads) k_wwalk_batch(const DecodeParams* ps,
@@ -842,7 +1348,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_wwalk_batch(const DecodeParams
     __shared__ DecodeParams sp;
     const BatchItem it = items[blockIdx.x];
     load_params(sp, ps + it.stream);
-    wwalk_body(sp);
+    if (sp.cap_bytes) wwalk_body<true>(sp);
+    else wwalk_body<false>(sp);
 }
 
 // The batch ticket hands out items in list order; the list holds each
@@ -874,7 +1381,7 @@ __global__ void __launch_bounds__(kFinalThreads) k_final_batch(const DecodeParam
 
 struct AuxLayout {
     size_t rec_g, rec_w, m, delta, Mpre, Dpre, status, tab_sync, tab_sym, scan_tiles,
-        scan_flags, walk_jobs, total;
+        scan_flags, walk_jobs, cap_valid, fb_list, cap, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
@@ -895,9 +1402,16 @@ static uint32_t walk_cap(const mans_cfg& c) {
     return std::max<uint32_t>(1, std::min<uint32_t>(cap, c.region_blocks - 1));
 }
 
-static size_t walk_smem(uint32_t L) {
+// Shared memory of a G-pass CTA: table, lane rings, mbarriers and, with
+// capture, the warps' capture rings (16-byte aligned).
+static size_t sync_smem(uint32_t L, uint32_t threads, bool capture) {
+    return (((size_t) L * 8 + 15) & ~(size_t) 15) + (size_t) threads * kRingStride +
+           (threads / 32) * 40 + (capture ? 16 + (size_t) (threads / 32) * kCapWarpBytes : 0);
+}
+
+static size_t walk_smem(uint32_t L, bool capture) {
     return (((size_t) L * 8 + 15) & ~(size_t) 15) + (size_t) kWalkThreads * kWindowStride +
-           (kWalkThreads / 32) * 8;
+           (kWalkThreads / 32) * 8 + (capture ? 16 + (kWalkThreads / 32) * kCapWarpBytes : 0);
 }
 
 // Opts the kernels in to large dynamic shared memory, once per device.
@@ -909,10 +1423,14 @@ static void set_kernel_attributes() {
     std::lock_guard<std::mutex> lock(mu);
     if (dev < 64 && ((done >> dev) & 1)) return;
     cudaFuncSetAttribute(k_prep, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_gwalk, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_wwalk, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_gwalk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_gwalk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_wwalk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_wwalk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_final<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_final<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_final_fb<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_final_fb<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_prep_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_gwalk_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_wwalk_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
@@ -920,7 +1438,7 @@ static void set_kernel_attributes() {
     if (dev < 64) done |= 1ull << dev;
 }
 
-static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax) {
+static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax, size_t cap_bytes) {
     AuxLayout a;
     size_t o = 0;
     a.status = o; o += 256;
@@ -934,8 +1452,12 @@ static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax) {
     a.Dpre = o; o += align256(nreg * 8);
     const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
     a.scan_tiles = o; o += align256(ntiles * sizeof(ScanTile));
-    a.scan_flags = o; o += align256((ntiles + 3) * 4);   // flags, ticket, job count, next job
+    // flags, ticket, job count, next job, fallback warp count
+    a.scan_flags = o; o += align256((ntiles + 4) * 4);
     a.walk_jobs = o; o += align256(nreg * sizeof(WJob));
+    a.cap_valid = o; o += cap_bytes ? align256(nreg * 4) : 0;
+    a.fb_list = o; o += cap_bytes ? align256((nblk + 31) / 32 * 4) : 0;
+    a.cap = o; o += cap_bytes ? align256(nreg * cap_bytes + 16) : 0;
     a.total = o;
     return a;
 }
@@ -1003,12 +1525,23 @@ static double mean_meeting_units(uint32_t L, double bits_per_symbol) {
     return d1 + u * (d4 - d1);
 }
 
+// Symbol capture (MANS_DECODE_NO_CAPTURE): from this many bits per symbol
+// on average zero-bit runs are rare, so the sync passes lose little by
+// decoding symbol by symbol, and a half block holds few enough symbols for
+// a lane's capture ring.
+constexpr double kCaptureMinBits = 2.0;
+constexpr uint32_t kCaptureMaxL = 1024;   // larger tables leave too little shared memory
+
 int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
               mans_cfg* out) {
     if (!out || n_units == 0 || L < 2 || L > kMaxStates) return MANS_ERR_ARG;
-    mans_cfg c = {0, 0, 0, 0};
+    mans_cfg c = {0, 0, 0, 0, 0, 0};
     if (hint) c = *hint;
     const double sym_per_unit = n_out ? (double) n_out / (double) n_units : 1.0;
+    const double bps = 32.0 / std::max(sym_per_unit, 1e-3);
+    const bool capture = c.capture_bytes != 0 ||
+                         (!(c.flags & MANS_DECODE_NO_CAPTURE) && n_out > 0 && L <= kCaptureMaxL &&
+                          bps >= kCaptureMinBits);
     if (c.block_units == 0) {
         // about 128 symbols per block
         uint64_t b = (uint64_t) (128.0 / std::max(sym_per_unit, 1e-3));
@@ -1030,12 +1563,14 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
     // three mean meeting distances and 512 units (2048 for L > 1024; more
     // when three meeting distances are longer): measured over 0.67 .. 8.6
     // bits per symbol and L = 1024 / 4096, between about 2.5 and 4 meeting
-    // distances is best.
+    // distances is best.  With capture the G pass holds 16 warps per SM,
+    // so R may grow to 1024 units to keep that one wave.
     const uint64_t tail = std::max<uint64_t>(256, 4ull * L);
+    const double meet = mean_meeting_units(L, bps);
     if (c.region_blocks == 0) {
         const uint64_t lanes = 152ull * 16 * 32;
-        const uint64_t r_sync = (uint64_t) (3.0 * mean_meeting_units(L, 32.0 / std::max(sym_per_unit, 1e-3)));
-        const uint64_t r_max = std::max<uint64_t>(L <= 1024 ? 512 : 2048, r_sync);
+        const uint64_t r_sync = (uint64_t) (3.0 * meet);
+        const uint64_t r_max = std::max<uint64_t>(capture ? 1024 : (L <= 1024 ? 512 : 2048), r_sync);
         uint64_t R = (n_units + lanes - 1) / lanes;
         R = std::min<uint64_t>(std::max<uint64_t>(R, std::max<uint64_t>(r_sync, 64)), r_max);
         // an odd block count keeps lanes of a warp (one region each) off
@@ -1048,6 +1583,15 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
     }
     if (c.threads == 0) c.threads = 128;
     c.threads = std::min<uint32_t>(128, std::max<uint32_t>(32, c.threads & ~31u));
+    if (capture && c.capture_bytes == 0) {
+        // the region's symbols and those of the first stretch of its merge
+        // walk, with a quarter to spare; blocks past the slice are decoded
+        const double R = (double) c.region_blocks * c.block_units;
+        const double walk = std::min(R, std::max((double) kWalkCapUnits, 3.0 * meet));
+        const double bytes = sym_per_unit * (R + walk) * 1.25 + 64.0;
+        c.capture_bytes = (uint32_t) std::min(bytes, (double) (1u << 30));
+    }
+    c.capture_bytes = (c.capture_bytes + 15) & ~15u;
     *out = c;
     return MANS_OK;
 }
@@ -1057,12 +1601,14 @@ size_t mans_aux_size(size_t n_units, const mans_cfg* cfg) {
         return 0;
     const size_t nblk = num_blocks(n_units, cfg->block_units);
     const size_t nreg = (nblk + cfg->region_blocks - 1) / cfg->region_blocks;
-    return layout_for(nblk, nreg, cfg->walk_slots).total;
+    return layout_for(nblk, nreg, cfg->walk_slots, cfg->capture_bytes).total;
 }
 
 size_t mans_aux_size_max(size_t n_units) {
-    // smallest blocks (4 units), fewest blocks per region (8), most slots
-    mans_cfg c = {4, 8, kMaxWalkSlots, 128};
+    // smallest blocks (4 units), fewest blocks per region (8), most slots,
+    // no capture (a decode whose plan captures into less memory than it
+    // needs runs without)
+    mans_cfg c = {4, 8, kMaxWalkSlots, 128, 0, 0};
     return mans_aux_size(n_units, &c);
 }
 
@@ -1099,7 +1645,7 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     if (rc != MANS_OK) return rc;
     const size_t nblk = num_blocks(n_units, cfg.block_units);
     const size_t nreg = (nblk + cfg.region_blocks - 1) / cfg.region_blocks;
-    const AuxLayout lay = layout_for(nblk, nreg, cfg.walk_slots);
+    const AuxLayout lay = layout_for(nblk, nreg, cfg.walk_slots, cfg.capture_bytes);
     if (aux_bytes < lay.total) return MANS_ERR_AUX_SMALL;
     if ((uint64_t) nblk * cfg.block_units * 32 >= (1ull << 40)) return MANS_ERR_ARG;
 
@@ -1133,10 +1679,15 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     p.nreg = (uint32_t) nreg;
     p.wcap = walk_cap(cfg);
     p.flags = cfg.flags & MANS_DECODE_SOURCE_ORDER;
+    p.cap_bytes = cfg.capture_bytes;
+    p.cap = cfg.capture_bytes ? (uint8_t*) (base + lay.cap) : nullptr;
+    p.cap_valid = cfg.capture_bytes ? (uint32_t*) (base + lay.cap_valid) : nullptr;
+    p.fb_list = cfg.capture_bytes ? (uint32_t*) (base + lay.fb_list) : nullptr;
+    const bool capture = cfg.capture_bytes != 0;
 
     const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
     if (cudaMemsetAsync(p.status, 0, sizeof(uint32_t), st) != cudaSuccess ||
-        cudaMemsetAsync(base + lay.scan_flags, 0, (ntiles + 3) * 4, st) != cudaSuccess)
+        cudaMemsetAsync(base + lay.scan_flags, 0, (ntiles + 4) * 4, st) != cudaSuccess)
         return MANS_ERR_CUDA;
     const size_t smem = ((size_t) L * sizeof(uint2) + 15) & ~(size_t) 15;
     set_kernel_attributes();
@@ -1145,9 +1696,9 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     uint64_t cap = (uint64_t) (per_unit * 32.0 * cfg.block_units * 1.5) + 256;
     cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
     p.stage_cap = (uint32_t) ((cap + 15) & ~(uint64_t) 15);
-    const uint32_t gthreads = L >= 4096 ? kSyncThreadsMax : kSyncThreads;
-    const size_t smem_sync = smem + (size_t) gthreads * kRingStride + (gthreads / 32) * 40;
-    const size_t smem_walk = walk_smem(L);
+    const uint32_t gthreads = (capture || L >= 4096) ? kSyncThreadsMax : kSyncThreads;
+    const size_t smem_sync = sync_smem(L, gthreads, capture);
+    const size_t smem_walk = walk_smem(L, capture);
     const uint32_t tile_bytes = (cfg.block_units + 4) * 4;
     const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
     const size_t per_warp_final = (size_t) 32 * tile_stride + 16 + p.stage_cap + 16;
@@ -1155,19 +1706,38 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     timing_mark(0, st);
     k_prep<<<1, 1024, (size_t) L * 12, st>>>(p);
     timing_mark(1, st);
-    k_gwalk<<<(unsigned) ((nreg + gthreads - 1) / gthreads), gthreads, smem_sync, st>>>(p);
+    const unsigned gg = (unsigned) ((nreg + gthreads - 1) / gthreads);
+    if (capture) k_gwalk<true><<<gg, gthreads, smem_sync, st>>>(p);
+    else k_gwalk<false><<<gg, gthreads, smem_sync, st>>>(p);
     timing_mark(2, st);
     uint32_t launches = 4;
     if (const uint32_t ww = walk_ctas(nreg)) {
-        k_wwalk<<<ww, kWalkThreads, smem_walk, st>>>(p);
+        if (capture) k_wwalk<true><<<ww, kWalkThreads, smem_walk, st>>>(p);
+        else k_wwalk<false><<<ww, kWalkThreads, smem_walk, st>>>(p);
         ++launches;
     }
     timing_mark(3, st);
     k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(p);
     timing_mark(4, st);
     const unsigned gf = (unsigned) ((nblk + kFinalThreads - 1) / kFinalThreads);
-    if (p.flags & MANS_DECODE_SOURCE_ORDER) k_final<true><<<gf, kFinalThreads, smem_final, st>>>(p);
-    else k_final<false><<<gf, kFinalThreads, smem_final, st>>>(p);
+    const bool rev = (p.flags & MANS_DECODE_SOURCE_ORDER) != 0;
+    if (capture) {
+        // copy the captured warps, then decode the listed ones
+        const unsigned gc = (unsigned) ((nblk + kCopyThreads - 1) / kCopyThreads);
+        const unsigned gfb = std::min<unsigned>(gf, 152 * 3);
+        if (rev) {
+            k_copy<true><<<gc, kCopyThreads, 0, st>>>(p);
+            k_final_fb<true><<<gfb, kFinalThreads, smem_final, st>>>(p);
+        } else {
+            k_copy<false><<<gc, kCopyThreads, 0, st>>>(p);
+            k_final_fb<false><<<gfb, kFinalThreads, smem_final, st>>>(p);
+        }
+        ++launches;
+    } else if (rev) {
+        k_final<true><<<gf, kFinalThreads, smem_final, st>>>(p);
+    } else {
+        k_final<false><<<gf, kFinalThreads, smem_final, st>>>(p);
+    }
     timing_mark(5, st);
     if (g_timing.on && g_timing.used < g_timing.cap) ++g_timing.used;
     g_last_launches = launches;
@@ -1231,15 +1801,20 @@ int mans_decode_sync(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
                      uint32_t first_state, uint32_t first_bit, void* d_aux,
                      size_t aux_bytes, const mans_cfg* hint, void* stream,
                      uint32_t* status_out) {
-    mans_cfg c = {0, 0, 0, 0};
+    mans_cfg c = {0, 0, 0, 0, 0, 0};
     if (hint) c = *hint;
     mans_cfg plan;
     uint32_t st = 0;
-    for (int attempt = 0; attempt < 6; ++attempt) {
+    for (int attempt = 0; attempt < 8; ++attempt) {
         int rc = mans_plan(n_units, n_out, L, &c, &plan);
         if (rc != MANS_OK) return rc;
         if (mans_aux_size(n_units, &plan) > aux_bytes) {
-            // fewer slots fit in the same memory
+            if (plan.capture_bytes) {
+                // no capture first, then fewer slots, fit in the same memory
+                c.capture_bytes = 0;
+                c.flags |= MANS_DECODE_NO_CAPTURE;
+                continue;
+            }
             if (plan.walk_slots > 1) { c = plan; c.walk_slots = plan.walk_slots / 2; continue; }
             return MANS_ERR_AUX_SMALL;
         }
@@ -1250,9 +1825,11 @@ int mans_decode_sync(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
         rc = mans_aux_status(d_aux, stream, &st);
         if (rc != MANS_OK) return rc;
         if (!(st & MANS_DEV_SYNC_OVERFLOW)) break;
-        // a walk outran its slots: longer regions, same slot count
+        // a walk outran its slots: longer regions, same slot count (and a
+        // capture slice sized for them)
         c = plan;
         c.region_blocks = plan.region_blocks * 4;
+        c.capture_bytes = 0;
     }
     if (status_out) *status_out = st;
     return mans_status_code(st);
@@ -1283,7 +1860,7 @@ struct BatchLayout {
 };
 
 static size_t stream_data_bytes(const BatchStreamPlan& sp) {
-    const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots);
+    const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots, sp.cfg.capture_bytes);
     return a.total;
 }
 
@@ -1308,7 +1885,10 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
             d[i].first_state < d[i].L || d[i].first_state >= 2 * d[i].L || d[i].first_bit > 32 ||
             ((uintptr_t) d[i].d_units & 15) != 0)
             return MANS_ERR_ARG;
-        int rc = mans_plan(d[i].n_units, d[i].n_out, d[i].L, hint, &sp.cfg);
+        mans_cfg h = {0, 0, 0, 0, 0, 0};
+        if (hint) h = *hint;
+        h.flags |= d[i].flags & MANS_DECODE_NO_CAPTURE;
+        int rc = mans_plan(d[i].n_units, d[i].n_out, d[i].L, &h, &sp.cfg);
         if (rc != MANS_OK) return rc;
         sp.cfg.flags = d[i].flags & MANS_DECODE_SOURCE_ORDER;
         sp.nblk = num_blocks(d[i].n_units, sp.cfg.block_units);
@@ -1317,17 +1897,17 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
         sp.data_off = data;
         data += align256(stream_data_bytes(sp));
         sp.flags_off = flag_words;
-        flag_words += sp.ntiles + 3;
+        flag_words += sp.ntiles + 4;
         sp.stage_cap = stage_cap_for((double) d[i].n_out / (double) d[i].n_units,
                                      sp.cfg.block_units);
         lay.n_sync += (sp.nreg + kSyncThreads - 1) / kSyncThreads;
         lay.n_walk += walk_ctas(sp.nreg);
-        lay.smem_walk = std::max(lay.smem_walk, walk_smem(d[i].L));
+        lay.smem_walk = std::max(lay.smem_walk, walk_smem(d[i].L, sp.cfg.capture_bytes != 0));
         lay.n_scan += sp.ntiles;
         lay.n_final += (sp.nblk + kFinalThreads - 1) / kFinalThreads;
         const size_t tab = ((size_t) d[i].L * 8 + 15) & ~(size_t) 15;
-        lay.smem_sync = std::max(lay.smem_sync, tab + (size_t) kSyncThreads * kRingStride +
-                                                    (kSyncThreads / 32) * 40);
+        lay.smem_sync = std::max(lay.smem_sync,
+                                 sync_smem(d[i].L, kSyncThreads, sp.cfg.capture_bytes != 0));
         const uint32_t tile_bytes = (sp.cfg.block_units + 4) * 4;
         const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
         lay.smem_final = std::max(lay.smem_final,
@@ -1438,7 +2018,7 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         p.status = (uint32_t*) (b->base + b->lay.status) + i;
         if (!sp.active) continue;
         const mans_stream_desc& d = streams[i];
-        const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots);
+        const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots, sp.cfg.capture_bytes);
         char* slice = slices ? (char*) slices[i] : b->base + b->lay.data + sp.data_off;
         if (!slice || ((uintptr_t) slice & 255) != 0) { mans_batch_destroy(b); return MANS_ERR_ARG; }
         b->slice[i] = slice;
@@ -1469,6 +2049,10 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         p.stage_cap = sp.stage_cap;
         p.wcap = walk_cap(sp.cfg);
         p.flags = d.flags & MANS_DECODE_SOURCE_ORDER;
+        p.cap_bytes = sp.cfg.capture_bytes;
+        p.cap = sp.cfg.capture_bytes ? (uint8_t*) (slice + a.cap) : nullptr;
+        p.cap_valid = sp.cfg.capture_bytes ? (uint32_t*) (slice + a.cap_valid) : nullptr;
+        p.fb_list = sp.cfg.capture_bytes ? (uint32_t*) (slice + a.fb_list) : nullptr;
         for (size_t r = 0; r < sp.nreg; r += kSyncThreads) b->items[is++] = {i, (uint32_t) r, 0, 0};
         for (uint32_t c = 0; c < walk_ctas(sp.nreg); ++c) b->items[iw++] = {i, c, 0, 0};
         for (size_t t = 0; t < sp.ntiles; ++t) b->items[ic++] = {i, (uint32_t) t, 0, 0};

@@ -67,8 +67,14 @@ int mans_decode_noalloc(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     if (status_out) *status_out = 0;
     if (n_out == 0) return MANS_OK;
     mans_cfg plan;
-    const int rc = mans_plan(n_units, n_out, L, nullptr, &plan);
+    int rc = mans_plan(n_units, n_out, L, nullptr, &plan);
     if (rc != MANS_OK) return rc;
+    if (plan.capture_bytes && mans_aux_size(n_units, &plan) > kScratchBytes) {
+        // the capture slices do not fit: decode every block in the final pass
+        mans_cfg hint = {0, 0, 0, 0, MANS_DECODE_NO_CAPTURE, 0};
+        rc = mans_plan(n_units, n_out, L, &hint, &plan);
+        if (rc != MANS_OK) return rc;
+    }
     if (mans_aux_size(n_units, &plan) > kScratchBytes) return MANS_ERR_AUX_SMALL;
     void* scratch = nullptr;
     const int sc = scratch_address(&scratch);

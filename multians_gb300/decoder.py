@@ -60,6 +60,15 @@ class CUHDGPUDecoderMemory:
                                    device=self.device or "cuda")
         return self
 
+    def reserve(self, nbytes: int):
+        """Grows the workspace to ``nbytes`` (a plan that captures symbols
+        needs room that scales with the output size)."""
+        self.allocate()
+        if self.buf.numel() < nbytes:
+            torch = _torch()
+            self.buf = torch.empty(nbytes, dtype=torch.uint8, device=self.buf.device)
+        return self
+
     def free(self):
         self.buf = None
 
@@ -78,8 +87,9 @@ class CUHDGPUDecoder:
         packed CUHDCodetableItem words, ``output`` a CUDA uint8 tensor.
         Synchronous; returns the device status bits."""
         del max_codeword_length  # unused by the reference too (.cu:217)
-        if aux.get() is None:
-            aux.allocate()
+        from ._lib import aux_size, plan
+        aux.reserve(aux_size(int(input_size), plan(int(input_size), int(output_size),
+                                                   int(number_of_states), {})))
         st = ctypes.c_uint32(0)
         rc = lib().mans_decode_sync(
             _dev_ptr(input), int(input_size), _dev_ptr(output), int(output_size),
@@ -131,10 +141,9 @@ def decode(units, n_units: int, n_out: int, table, first_state: int, first_bit: 
     if out is None:
         out = torch.empty(max(1, n_out), dtype=torch.uint8, device=dev)
     if aux is None:
-        need = aux_size_max(max(1, n_units))
-        if cfg:
-            from ._lib import plan, aux_size
-            need = max(need, aux_size(n_units, plan(n_units, n_out, L, cfg)))
+        from ._lib import plan, aux_size
+        need = max(aux_size_max(max(1, n_units)),
+                   aux_size(n_units, plan(n_units, n_out, L, cfg or {})))
         aux = torch.empty(need, dtype=torch.uint8, device=dev)
     st = ctypes.c_uint32(0)
     rc = lib().mans_decode_sync(_dev_ptr(units), int(n_units), _dev_ptr(out), int(n_out),

@@ -46,12 +46,34 @@ def test_version(mg):
 
 
 def test_plan_and_aux_sizes(mg):
-    p = mg.plan(50_000_000, 268_435_456, 1024)
+    p = mg.plan(50_000_000, 268_435_456, 1024, {"flags": mg.DECODE_NO_CAPTURE})
     assert p["block_units"] >= 4 and p["region_blocks"] >= 1 and p["walk_slots"] >= 1
+    assert p["capture_bytes"] == 0
     need = mg.aux_size(50_000_000, p)
     assert 0 < need <= mg.aux_size_max(50_000_000)
     small = mg.plan(1000, 5000, 4096)
+    assert small["capture_bytes"] == 0   # 6.4 bits/symbol but L > 1024
     assert mg.aux_size(1000, small) <= mg.aux_size_max(1000)
+
+
+def test_capture_plan(mg):
+    """6 bits per symbol at L = 1024 captures: one slice per region holding
+    the region's symbols and a walk's with room to spare; low-entropy
+    streams and L > 1024 do not."""
+    n_units, n_out = 50_000_000, 268_435_456
+    p = mg.plan(n_units, n_out, 1024)
+    R = p["block_units"] * p["region_blocks"]
+    per_region = n_out / n_units * R
+    assert p["capture_bytes"] % 16 == 0 and p["capture_bytes"] >= 1.25 * per_region
+    nblk = n_units // p["block_units"] + 1
+    nreg = -(-nblk // p["region_blocks"])
+    assert nreg <= 152 * 16 * 32   # the capture G pass keeps one wave
+    extra = mg.aux_size(n_units, p) - mg.aux_size(n_units, dict(p, capture_bytes=0))
+    assert extra >= nreg * p["capture_bytes"]
+    assert mg.plan(1_000_000, 20_000_000, 1024)["capture_bytes"] == 0    # 1.6 bits/symbol
+    assert mg.plan(1_000_000, 5_000_000, 4096)["capture_bytes"] == 0
+    forced = mg.plan(1_000_000, 20_000_000, 1024, {"capture_bytes": 1000})
+    assert forced["capture_bytes"] == 1008
 
 
 def test_table_check(mg, oracle_lib):
