@@ -12,7 +12,10 @@ seeded synthetic uint8 symbols, the reference's table generator and encoder
           resident in HBM; each step is one full decode (four kernels).
   e2e     the same metric through the public C ABI with host buffers: per
           step the pinned-host units and table go host->device, the decode
-          runs, the decoded bytes come back device->host.
+          runs, the decoded bytes come back device->host; steps pipelined
+          over two buffer sets (input copy, decode and output copy of
+          neighbouring steps overlap), with the one-stream serial figure
+          beside it.
   roofline  the dominant kernel: algorithmic bytes per launch / its mean
           launch time (CUDA events around every kernel in the timed
           region), against the measured HBM copy bandwidth.
@@ -54,6 +57,8 @@ def parse():
     ap.add_argument("--L", type=int, default=1024)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-capture", action="store_true",
+                    help="decode without symbol capture (MANS_DECODE_NO_CAPTURE)")
     ap.add_argument("--cpu-sample-mb", type=float, default=32.0)
     ap.add_argument("--rate", type=float, default=0.0,
                     help="served workload: Poisson arrival rate, requests/s (0 = 50000)")
@@ -241,7 +246,7 @@ def run_ours(args, ws, rank, local):
     table = table_h.to(dev)
     out = torch.empty(n, dtype=torch.uint8, device=dev)
     out_h = torch.empty(n, dtype=torch.uint8).pin_memory()
-    cfg = mg.plan(st.n_units, n, st.L)
+    cfg = mg.plan(st.n_units, n, st.L, {"flags": mg.DECODE_NO_CAPTURE} if args.no_capture else None)
     aux = torch.empty(mg.aux_size(st.n_units, cfg), dtype=torch.uint8, device=dev)
     want = torch.from_numpy(np.ascontiguousarray(st.symbols[::-1])).to(dev)
     stream = torch.cuda.current_stream(dev)
@@ -285,7 +290,13 @@ def run_ours(args, ws, rank, local):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
 
-    # e2e: host buffers through the C ABI, copies inside the timed region
+    # e2e: host buffers through the C ABI, copies inside the timed region.
+    # Serial: per step H2D, decode, D2H on one stream.  Pipelined, the way a
+    # streaming caller runs it: two device and two host buffer sets; step
+    # i's H2D on an input copy stream, its decode on the compute stream and
+    # its D2H on an output copy stream, each waiting only on what it reads
+    # or overwrites, so step i+1's input copy and step i-1's output copy run
+    # under step i's decode.  Every step still moves its own bytes.
     h2d = st.units.nbytes + st.table.nbytes
     d2h = n
     e2e_steps = max(3, min(args.steps, 10))
@@ -304,8 +315,51 @@ def run_ours(args, ws, rank, local):
         out_h.copy_(out, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize(dev)
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_serial_ms = e0.elapsed_time(e1) / e2e_steps
     e2e_ok = bool(np.array_equal(out_h.numpy(), st.symbols[::-1]))
+
+    units2 = [units, torch.empty_like(units)]
+    table2 = [table, torch.empty_like(table)]
+    out2 = [out, torch.empty_like(out)]
+    out_h2 = [out_h, torch.empty(n, dtype=torch.uint8).pin_memory()]
+    s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def pipelined(steps):
+        ev = lambda: torch.cuda.Event(enable_timing=False)  # noqa: E731
+        in_done, dec_done, out_done = [], [], []
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(s_in)
+        for i in range(steps):
+            k = i & 1
+            with torch.cuda.stream(s_in):
+                if i >= 2:
+                    s_in.wait_event(dec_done[i - 2])   # decode i-2 read units[k]
+                units2[k].copy_(units_h, non_blocking=True)
+                table2[k].copy_(table_h, non_blocking=True)
+                in_done.append(ev())
+                in_done[i].record(s_in)
+            stream.wait_event(in_done[i])
+            if i >= 2:
+                stream.wait_event(out_done[i - 2])     # D2H i-2 read out[k]
+            decode_async(units2[k], st.n_units, out2[k], n, table2[k], st.L, st.first_state,
+                         st.first_bit, aux, cfg, stream=stream)
+            dec_done.append(ev())
+            dec_done[i].record(stream)
+            s_out.wait_event(dec_done[i])
+            with torch.cuda.stream(s_out):
+                out_h2[k].copy_(out2[k], non_blocking=True)
+                out_done.append(ev())
+                out_done[i].record(s_out)
+        t1.record(s_out)
+        torch.cuda.synchronize(dev)
+        return t0.elapsed_time(t1) / steps, (steps - 1) & 1
+
+    pipelined(2)
+    e2e_ms, last = pipelined(e2e_steps)
+    e2e_ok = e2e_ok and bool(np.array_equal(out_h2[last].numpy(), st.symbols[::-1]))
+    e2e_ok = e2e_ok and aux_status(aux, stream) == 0
+    del units2, table2, out2, out_h2
 
     if rank != 0:
         if ws > 1:
@@ -362,7 +416,9 @@ def run_ours(args, ws, rank, local):
                      "alg_bytes_per_launch": alg},
         "cpu_baseline": cpu,
         "e2e": {"value": round(ws * n / (e2e_ms / 1e3) / 1e9, 3), "unit": "GB/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "bit_exact": e2e_ok},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "bit_exact": e2e_ok,
+                "pipelined": "2 buffer sets; H2D, decode, D2H on 3 streams",
+                "serial_value": round(ws * n / (e2e_serial_ms / 1e3) / 1e9, 3)},
         "gpu_launches": launches_per * args.steps,
         "clocks": clk.summary(),
         "gen_seconds": round(gen_s, 2),

@@ -69,7 +69,9 @@ typedef struct {
 #define MANS_DECODE_SOURCE_ORDER 0x1u
 
 /* Symbol capture.  When the stream has at least two bits per symbol on
- * average (few zero-bit codewords) and L <= 1024, the planner gives every sync
+ * average (few zero-bit codewords), L <= 1024 and at least 16 Mi units (64
+ * MiB compressed; below that the capture's fixed cost outweighs what it
+ * saves), or when capture_bytes is given, the planner gives every sync
  * region capture_bytes of workspace: the sync passes, which decode each
  * region once from a guessed state anyway, keep the symbols they decode
  * there, and the final pass copies every block whose owning trajectory was
@@ -217,6 +219,7 @@ typedef struct {
 #define MANS_REQ_CONTAINER 0x4u     /* units points at a host container of n_units
                                        bytes; table, n_out, first_state / first_bit
                                        come from it (out must hold n_symbols) */
+#define MANS_REQ_NO_CAPTURE 0x8u    /* decode without symbol capture (MANS_DECODE_NO_CAPTURE) */
 
 typedef struct {
     const uint32_t* units;    /* CUHDInputBuffer order; 16-byte aligned if device */

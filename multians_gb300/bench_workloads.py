@@ -73,7 +73,8 @@ def run_batched(args, ws, rank, local):
     stream = torch.cuda.current_stream(dev)
 
     # batched decode
-    descs = [batch.desc(u, st.n_units, o, st.n, t, st.L, st.first_state, st.first_bit)
+    cap = not getattr(args, "no_capture", False)
+    descs = [batch.desc(u, st.n_units, o, st.n, t, st.L, st.first_state, st.first_bit, capture=cap)
              for st, u, t, o in zip(sts, units, tables, outs)]
     b = batch.Batch(descs)
     for _ in range(max(3, args.warmup)):
@@ -101,7 +102,8 @@ def run_batched(args, ws, rank, local):
     batch_ms = evs[0].elapsed_time(evs[-1]) / steps
 
     # loop of plain decodes over the same streams (workspaces allocated up front)
-    plans = [mg.plan(st.n_units, st.n, st.L) for st in sts]
+    hint = None if cap else {"flags": mg.DECODE_NO_CAPTURE}
+    plans = [mg.plan(st.n_units, st.n, st.L, hint) for st in sts]
     auxes = [torch.empty(mg.aux_size(st.n_units, p), dtype=torch.uint8, device=dev)
              for st, p in zip(sts, plans)]
 

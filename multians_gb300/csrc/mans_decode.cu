@@ -1117,6 +1117,7 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
 // short chain of global loads (owners and records, issued together for
 // walk depths up to 2, then the symbols) and 16-byte stores.
 constexpr uint32_t kCopyThreads = 256;
+static_assert(kCopyThreads == kFinalThreads, "batch items give both kernels the same CTA blocks");
 
 struct CopyEntry {
     unsigned long long off;   // output offset of the block's first symbol
@@ -1367,13 +1368,33 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_batch(const DecodeParams*
     scan_body(sp, it.index);
 }
 
+// Final pass of a batch: streams with capture copy here first (k_copy_batch)
+// and decode only their listed warps in k_final_batch; the others decode
+// every block in k_final_batch.
+__global__ void __launch_bounds__(kCopyThreads) k_copy_batch(const DecodeParams* ps,
+                                                             const BatchItem* items) {
+    __shared__ DecodeParams sp;
+    const BatchItem it = items[blockIdx.x];
+    load_params(sp, ps + it.stream);
+    if (!sp.cap_bytes) return;
+    if (sp.flags & MANS_DECODE_SOURCE_ORDER) copy_body<true>(sp, it.index, it.count);
+    else copy_body<false>(sp, it.index, it.count);
+}
+
 __global__ void __launch_bounds__(kFinalThreads) k_final_batch(const DecodeParams* ps,
                                                                const BatchItem* items) {
     __shared__ DecodeParams sp;
     const BatchItem it = items[blockIdx.x];
     load_params(sp, ps + it.stream);
-    if (sp.flags & MANS_DECODE_SOURCE_ORDER) final_body<true>(sp, it.index, it.count);
-    else final_body<false>(sp, it.index, it.count);
+    const bool rev = (sp.flags & MANS_DECODE_SOURCE_ORDER) != 0;
+    if (sp.cap_bytes) {
+        if (rev) final_fb_body<true>(sp, it.index, it.count);
+        else final_fb_body<false>(sp, it.index, it.count);
+    } else if (rev) {
+        final_body<true>(sp, it.index, it.count);
+    } else {
+        final_body<false>(sp, it.index, it.count);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1528,9 +1549,13 @@ static double mean_meeting_units(uint32_t L, double bits_per_symbol) {
 // Symbol capture (MANS_DECODE_NO_CAPTURE): from this many bits per symbol
 // on average zero-bit runs are rare, so the sync passes lose little by
 // decoding symbol by symbol, and a half block holds few enough symbols for
-// a lane's capture ring.
+// a lane's capture ring.  Capture costs the G pass a roughly fixed time
+// (measured 0.05 ms: its rings take shared memory, so fewer warps per SM)
+// and saves the final pass time in proportion to the output (0.8 us per
+// MiB at 6 bits per symbol): from 16 M units on it pays.
 constexpr double kCaptureMinBits = 2.0;
 constexpr uint32_t kCaptureMaxL = 1024;   // larger tables leave too little shared memory
+constexpr size_t kCaptureMinUnits = 16u << 20;
 
 int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
               mans_cfg* out) {
@@ -1539,9 +1564,11 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
     if (hint) c = *hint;
     const double sym_per_unit = n_out ? (double) n_out / (double) n_units : 1.0;
     const double bps = 32.0 / std::max(sym_per_unit, 1e-3);
-    const bool capture = c.capture_bytes != 0 ||
-                         (!(c.flags & MANS_DECODE_NO_CAPTURE) && n_out > 0 && L <= kCaptureMaxL &&
-                          bps >= kCaptureMinBits);
+    const bool capture = !(c.flags & MANS_DECODE_NO_CAPTURE) &&
+                         (c.capture_bytes != 0 ||
+                          (n_out > 0 && L <= kCaptureMaxL && bps >= kCaptureMinBits &&
+                           n_units >= kCaptureMinUnits));
+    if (!capture) c.capture_bytes = 0;
     if (c.block_units == 0) {
         // about 128 symbols per block
         uint64_t b = (uint64_t) (128.0 / std::max(sym_per_unit, 1e-3));
@@ -1696,7 +1723,12 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     uint64_t cap = (uint64_t) (per_unit * 32.0 * cfg.block_units * 1.5) + 256;
     cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
     p.stage_cap = (uint32_t) ((cap + 15) & ~(uint64_t) 15);
-    const uint32_t gthreads = (capture || L >= 4096) ? kSyncThreadsMax : kSyncThreads;
+    // G-pass CTAs: 256 threads share a table for L >= 4096; with capture 128
+    // (three CTAs, 12 warps per SM) while the regions fit that in one wave,
+    // else 256 (two CTAs, 16 warps)
+    const uint32_t gthreads =
+        capture ? (nreg <= 152ull * 3 * kSyncThreads ? kSyncThreads : kSyncThreadsMax)
+                : (L >= 4096 ? kSyncThreadsMax : kSyncThreads);
     const size_t smem_sync = sync_smem(L, gthreads, capture);
     const size_t smem_walk = walk_smem(L, capture);
     const uint32_t tile_bytes = (cfg.block_units + 4) * 4;
@@ -1856,6 +1888,7 @@ struct BatchStreamPlan {
 struct BatchLayout {
     size_t status, flags, ticket, params, items, data, total;
     size_t n_sync, n_walk, n_scan, n_final, n_items;
+    bool any_capture;
     size_t smem_sync, smem_walk, smem_final, smem_prep;
 };
 
@@ -1875,6 +1908,7 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
     plans.assign(n, BatchStreamPlan{});
     size_t data = 0, flag_words = 0;
     lay.n_sync = lay.n_walk = lay.n_scan = lay.n_final = 0;
+    lay.any_capture = false;
     lay.smem_sync = lay.smem_walk = lay.smem_final = lay.smem_prep = 0;
     for (uint32_t i = 0; i < n; ++i) {
         BatchStreamPlan& sp = plans[i];
@@ -1905,6 +1939,7 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
         lay.smem_walk = std::max(lay.smem_walk, walk_smem(d[i].L, sp.cfg.capture_bytes != 0));
         lay.n_scan += sp.ntiles;
         lay.n_final += (sp.nblk + kFinalThreads - 1) / kFinalThreads;
+        lay.any_capture |= sp.cfg.capture_bytes != 0;
         const size_t tab = ((size_t) d[i].L * 8 + 15) & ~(size_t) 15;
         lay.smem_sync = std::max(lay.smem_sync,
                                  sync_smem(d[i].L, kSyncThreads, sp.cfg.capture_bytes != 0));
@@ -2115,11 +2150,14 @@ int mans_batch_decode(mans_batch* b, void* stream) {
     if (L.n_scan)
         k_scan_batch<<<(unsigned) L.n_scan, kScanThreads, 0, st>>>(
             ps, items + L.n_sync + L.n_walk, (uint32_t*) (b->base + L.ticket));
+    if (L.n_final && L.any_capture)
+        k_copy_batch<<<(unsigned) L.n_final, kCopyThreads, 0, st>>>(
+            ps, items + L.n_sync + L.n_walk + L.n_scan);
     if (L.n_final)
         k_final_batch<<<(unsigned) L.n_final, kFinalThreads, L.smem_final, st>>>(
             ps, items + L.n_sync + L.n_walk + L.n_scan);
     g_last_launches = 1 + (L.n_sync ? 1 : 0) + (L.n_walk ? 1 : 0) + (L.n_scan ? 1 : 0) +
-                      (L.n_final ? 1 : 0);
+                      (L.n_final ? (L.any_capture ? 2 : 1) : 0);
     return cudaGetLastError() == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
 }
 

@@ -247,7 +247,8 @@ struct mans_server {
         d.L = L;
         d.first_state = r.first_state;
         d.first_bit = r.first_bit;
-        d.flags = (r.flags & MANS_REQ_SOURCE_ORDER) ? MANS_DECODE_SOURCE_ORDER : 0u;
+        d.flags = ((r.flags & MANS_REQ_SOURCE_ORDER) ? MANS_DECODE_SOURCE_ORDER : 0u) |
+                  ((r.flags & MANS_REQ_NO_CAPTURE) ? MANS_DECODE_NO_CAPTURE : 0u);
         size_t slice = 0;
         const int rc = mans_batch_slice_size(&d, nullptr, &slice);
         if (rc != MANS_OK) return rc;

@@ -21,6 +21,7 @@ from ._lib import MansError, check, lib
 REQ_DEVICE_IO = 0x1
 REQ_SOURCE_ORDER = 0x2
 REQ_CONTAINER = 0x4
+REQ_NO_CAPTURE = 0x8
 
 
 class ServerCfg(ctypes.Structure):
@@ -87,11 +88,12 @@ def now_ns() -> int:
 
 
 def request(units, n_units, out, n_out, table, first_state, first_bit, tag=0,
-            arrival_ns=0, device_io=False, source_order=False) -> RequestC:
+            arrival_ns=0, device_io=False, source_order=False, capture=True) -> RequestC:
     """A request from tensors (or raw addresses)."""
     up = units if isinstance(units, int) else units.data_ptr()
     op = out if isinstance(out, int) else out.data_ptr()
-    flags = (REQ_DEVICE_IO if device_io else 0) | (REQ_SOURCE_ORDER if source_order else 0)
+    flags = ((REQ_DEVICE_IO if device_io else 0) | (REQ_SOURCE_ORDER if source_order else 0) |
+             (0 if capture else REQ_NO_CAPTURE))
     return RequestC(up, int(n_units), op, int(n_out), int(table), int(first_state),
                     int(first_bit), flags, int(tag), int(arrival_ns))
 

@@ -64,7 +64,7 @@ def _np_dtype(cstruct):
 class Replay:
     """Prebuilt request array for one trace and one buffer set."""
 
-    def __init__(self, serve, entry, units_ptr, out_ptr, sts, tids, device_io):
+    def __init__(self, serve, entry, units_ptr, out_ptr, sts, tids, device_io, capture=True):
         self.serve = serve
         n = entry.size
         self.arr = (serve.RequestC * n)()
@@ -76,7 +76,8 @@ class Replay:
         v["table"] = np.asarray(tids, dtype=np.uint32)[entry]
         v["first_state"] = np.array([st.first_state for st in sts], dtype=np.uint32)[entry]
         v["first_bit"] = np.array([st.first_bit for st in sts], dtype=np.uint32)[entry]
-        v["flags"] = serve.REQ_DEVICE_IO if device_io else 0
+        v["flags"] = ((serve.REQ_DEVICE_IO if device_io else 0) |
+                      (0 if capture else serve.REQ_NO_CAPTURE))
         v["tag"] = np.arange(n, dtype=np.uint64)
         self.view = v
         self.n = n
@@ -158,10 +159,11 @@ def run(args, ws, rank, local):
 
     srv = serve.Server(budget_bytes=budget)
     tids = [srv.add_table(st.table) for st in sts]
+    cap = not getattr(args, "no_capture", False)
     rp_dev = Replay(serve, entry, [t.data_ptr() for t in d_units], [t.data_ptr() for t in d_out],
-                    sts, tids, device_io=True)
+                    sts, tids, device_io=True, capture=cap)
     rp_host = Replay(serve, entry, [t.data_ptr() for t in h_units], [t.data_ptr() for t in h_out],
-                     sts, tids, device_io=False)
+                     sts, tids, device_io=False, capture=cap)
 
     # verification replay: waves with no stream twice, every output checked
     ok = True
@@ -210,7 +212,7 @@ def run(args, ws, rank, local):
     lat_rate = 0.5 * n_req / e2e_s
     entry_lat, offs_lat = trace(seed + 17, n_req, n_pool, lat_rate)
     rp_lat = Replay(serve, entry_lat, [t.data_ptr() for t in h_units],
-                    [t.data_ptr() for t in h_out], sts, tids, device_io=False)
+                    [t.data_ptr() for t in h_out], sts, tids, device_io=False, capture=cap)
     arr_l, done_l, status_l, _ = rp_lat.run(srv, offs_lat)
     all_ok &= bool((status_l == 0).all())
     lat = done_l.astype(np.int64) - arr_l.astype(np.int64)
@@ -220,7 +222,8 @@ def run(args, ws, rank, local):
     srv.close()
 
     # a request-at-a-time service with the plain decoder, on the verified prefix
-    plans = [mg.plan(st.n_units, st.n, st.L) for st in sts]
+    plans = [mg.plan(st.n_units, st.n, st.L, None if cap else {"flags": mg.DECODE_NO_CAPTURE})
+             for st in sts]
     tabs = [torch.from_numpy(st.table.view(np.int32)).to(dev) for st in sts]
     aux = torch.empty(max(mg.aux_size(st.n_units, p) for st, p in zip(sts, plans)),
                       dtype=torch.uint8, device=dev)

@@ -70,8 +70,9 @@ def test_capture_plan(mg):
     assert nreg <= 152 * 16 * 32   # the capture G pass keeps one wave
     extra = mg.aux_size(n_units, p) - mg.aux_size(n_units, dict(p, capture_bytes=0))
     assert extra >= nreg * p["capture_bytes"]
-    assert mg.plan(1_000_000, 20_000_000, 1024)["capture_bytes"] == 0    # 1.6 bits/symbol
-    assert mg.plan(1_000_000, 5_000_000, 4096)["capture_bytes"] == 0
+    assert mg.plan(20_000_000, 400_000_000, 1024)["capture_bytes"] == 0   # 1.6 bits/symbol
+    assert mg.plan(20_000_000, 100_000_000, 4096)["capture_bytes"] == 0
+    assert mg.plan(12_000_000, 64_000_000, 1024)["capture_bytes"] == 0    # short stream
     forced = mg.plan(1_000_000, 20_000_000, 1024, {"capture_bytes": 1000})
     assert forced["capture_bytes"] == 1008
 
