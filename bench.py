@@ -374,8 +374,11 @@ def run_ours(args, ws, rank, local):
     mean_k = {k: v / max(1, kern_n) for k, v in kern_ms.items()}
     dom = max(mean_k, key=lambda k: mean_k[k])
     # k_gwalk reads the stream once; k_wwalk's re-reads are overhead, not
-    # algorithmic bytes; k_final reads the stream and writes the symbols
-    alg = {"k_gwalk": comp_bytes, "k_wwalk": 0, "k_final": comp_bytes + n,
+    # algorithmic bytes; k_final writes the symbols (and without capture
+    # reads the stream again; with capture it reads the captured symbols,
+    # which like the G pass's capture writes are overhead)
+    captured = cfg.get("capture_bytes", 0) > 0
+    alg = {"k_gwalk": comp_bytes, "k_wwalk": 0, "k_final": n if captured else comp_bytes + n,
            "k_prep": st.L * 4, "k_scan": 0}[dom]
     achieved = alg / (mean_k[dom] / 1e3) / 1e9
     traffic = None

@@ -331,11 +331,15 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
         __syncwarp();
     }
 
-    SCursorLazy A;   // 16+ warps per SM: shared-memory wavefronts bound this pass
+    // the uncaptured pass is bound by shared-memory wavefronts (lazy unit
+    // loads); the capturing one by instruction issue (a unit load every step)
+    SCursorT<!kCap> A;
     uint32_t ca = 0;
+    // the capture rows start on a 4 KB boundary, so a row address is the
+    // lane's column OR the row offset (one logic operation per step)
     CapLane cl;
-    cl.col = ((tb + tab_bytes + blockDim.x * kRingStride + (blockDim.x >> 5) * 40 + 15) & ~15u) +
-             warp * kCapWarpBytes + lane * 4;
+    cl.col = ((tb + tab_bytes + blockDim.x * kRingStride + (blockDim.x >> 5) * 40 + 4095) &
+              ~4095u) + warp * kCapWarpBytes + lane * 4;
     cl.acc = 0;
     cl.done = 0;
     cl.on = kCap;
@@ -401,7 +405,7 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
                 uint32_t cs = ca << 5;   // 32 x count: its bits 7..11 pick the ring row
                 while (A.pos < be) {
                     cl.acc = __byte_perm(cl.acc, A.step(rs), 0x7321);
-                    sts32(cl.col + (cs & 0xF80u), cl.acc);
+                    sts32(cl.col | (cs & 0xF80u), cl.acc);
                     cs += 32;
                 }
                 ca = cs >> 5;
@@ -1424,10 +1428,11 @@ static uint32_t walk_cap(const mans_cfg& c) {
 }
 
 // Shared memory of a G-pass CTA: table, lane rings, mbarriers and, with
-// capture, the warps' capture rings (16-byte aligned).
+// capture, the warps' capture rings (4 KB aligned: up to 4 KB of slack;
+// two 256-thread CTAs at L = 1024 still fit an SM).
 static size_t sync_smem(uint32_t L, uint32_t threads, bool capture) {
     return (((size_t) L * 8 + 15) & ~(size_t) 15) + (size_t) threads * kRingStride +
-           (threads / 32) * 40 + (capture ? 16 + (size_t) (threads / 32) * kCapWarpBytes : 0);
+           (threads / 32) * 40 + (capture ? 4096 + (size_t) (threads / 32) * kCapWarpBytes : 0);
 }
 
 static size_t walk_smem(uint32_t L, bool capture) {
