@@ -1121,6 +1121,7 @@ __device__ __forceinline__ void final_body(const DecodeParams& p, uint32_t cta, 
 // short chain of global loads (owners and records, issued together for
 // walk depths up to 2, then the symbols) and 16-byte stores.
 constexpr uint32_t kCopyThreads = 256;
+constexpr uint32_t kCopyEarlyBlocks = 12;
 static_assert(kCopyThreads == kFinalThreads, "batch items give both kernels the same CTA blocks");
 
 struct CopyEntry {
@@ -1145,12 +1146,16 @@ __device__ __forceinline__ CopyEntry copy_entry(const DecodeParams& p, uint32_t 
     const uint32_t V0 = __ldg(p.cap_valid + r), V1 = __ldg(p.cap_valid + r1),
                    V2 = __ldg(p.cap_valid + r2);
     const uint2 g = __ldg(p.rec_g + b);
+    // blocks near their region's start are mostly owned by the previous
+    // region's walk: their walk record is loaded with the rest
+    const bool early = b - r * p.nb < kCopyEarlyBlocks;
+    const uint2 w1 = early ? __ldg(p.rec_w + (size_t) b * p.dmax) : make_uint2(0, 0);
     uint32_t d;
     if (M0 <= bs) d = 0;
     else if (r >= 1 && M1 <= bs) d = 1;
     else if (r >= 2 && p.dmax >= 2 && M2 <= bs) d = 2;
     else return e;   // a deeper owner (or none): left to the decoding kernel
-    const uint2 rec = d == 0 ? g : __ldg(p.rec_w + (size_t) b * p.dmax + (d - 1));
+    const uint2 rec = d == 0 ? g : ((d == 1 && early) ? w1 : __ldg(p.rec_w + (size_t) b * p.dmax + (d - 1)));
     e.off = (unsigned long long) ((d == 0 ? D0 : (d == 1 ? D1 : D2)) + (long long) rec.y);
     const bool own = d == 0 || rec.x == g.x;   // on Gamma_r's trajectory here
     e.cy = own ? g.y : rec.y;
