@@ -275,8 +275,11 @@ __device__ __forceinline__ void cap_flush(CapLane& cl, uint8_t* __restrict__ dst
 // Gamma_{k+1}'s record (read from L2, one block ahead).  A walk that has not
 // merged after kWalkCapUnits units, and the walk of the warp's last lane
 // (whose successor region belongs to another warp), go to the job list of
-// the merge-walk pass (k_wwalk).
-constexpr uint32_t kWalkCapUnits = 128;
+// the merge-walk pass (k_wwalk).  The cap trades the G pass's lane
+// efficiency (a warp waits for its longest walk) against the merge-walk
+// pass's load; measured at 256 MiB, 6 bits per symbol: 32 units 356 GB/s,
+// 64 units 370, 128 units 363.
+constexpr uint32_t kWalkCapUnits = 64;
 template <bool kCap>
 __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase) {
     extern __shared__ __align__(16) uint2 s_tab[];
