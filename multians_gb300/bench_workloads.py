@@ -100,6 +100,16 @@ def run_batched(args, ws, rank, local):
         torch.cuda.synchronize(dev)
     per_ms = sorted(evs[i].elapsed_time(evs[i + 1]) for i in range(steps))
     batch_ms = evs[0].elapsed_time(evs[-1]) / steps
+    # per-kernel split: the same batch launched without the graph, events
+    # around each kernel (outside the timed region)
+    from multians_gb300 import _lib
+    _lib.timing_enable(3)
+    for _ in range(3):
+        b.decode(stream)
+    torch.cuda.synchronize(dev)
+    kern_ms, kern_n = _lib.timing_collect()
+    _lib.timing_enable(0)
+    kernel_ms = {k: round(v / max(1, kern_n), 4) for k, v in kern_ms.items()}
 
     # loop of plain decodes over the same streams (workspaces allocated up front)
     hint = None if cap else {"flags": mg.DECODE_NO_CAPTURE}
@@ -163,6 +173,7 @@ def run_batched(args, ws, rank, local):
         "sync_overflow_streams": n_overflow, "streams_redone": n_redone,
         "latency_ms": {"p50": round(per_ms[len(per_ms) // 2], 4),
                        "p99": round(per_ms[min(len(per_ms) - 1, int(0.99 * len(per_ms)))], 4)},
+        "kernel_ms": kernel_ms,
         "loop_of_plain": {"ms": round(loop_ms, 3),
                           "value": round(total_sym / (loop_ms / 1e3) / 1e9, 3),
                           "speedup_batched_vs_loop": round(loop_ms / batch_ms, 3)},

@@ -516,7 +516,13 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
     const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
     uint32_t* const job_next = p.scan_flags + ntile + 2;   // next job to take
     const uint32_t njobs = *(volatile uint32_t*) (p.scan_flags + ntile + 1);
-    if (njobs == 0 || *(volatile uint32_t*) job_next >= njobs) return;   // nothing left
+    {   // nothing left: one thread decides for the CTA (other CTAs take jobs
+        // meanwhile), which then leaves as a whole
+        __shared__ uint32_t s_go;
+        if (threadIdx.x == 0) s_go = njobs != 0 && *(volatile uint32_t*) job_next < njobs;
+        __syncthreads();
+        if (!s_go) return;
+    }
     load_prepared(s_tab, kCap ? p.tab_sym : p.tab_sync, p.L);
     if (*(volatile uint32_t*) p.status & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE)) return;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -742,6 +748,8 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
             if (g_rec != ~0u && !(fl & kGFollow)) g_rec = (G.pos - bs) | (entry_index(G.a, tb) << 8);
         }
     }
+    __syncwarp();
+    if (lane == 0) mbar_inval(bar);   // every phase completed: free for the next stream
     if (timed_out) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
 }
 
@@ -1356,13 +1364,49 @@ __global__ void __launch_bounds__(kSyncThreads) k_gwalk_batch(const DecodeParams
     else gwalk_body<false>(sp, it.index);
 }
 
+// Merge walks of a batch.  After the G pass k_walk_items appends, per
+// stream, one item per 64 open walks (at most the stream's static share of
+// CTAs) to one list; a persistent grid then takes items through a ticket,
+// each CTA running the stream's walk pass (whose lanes take that stream's
+// jobs until its list is exhausted).  A launch with one CTA per region
+// group of every stream would run in waves, each as long as its longest
+// walk.
+__device__ __forceinline__ uint32_t walk_ctas_for(uint32_t nreg) {
+    if (nreg < 2) return 0;
+    return min((nreg - 1 + kWalkThreads - 1) / kWalkThreads, kWalkCtasMax);
+}
+
+__global__ void k_walk_items(const DecodeParams* ps, uint32_t n, uint32_t* list,
+                             uint32_t* count) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const DecodeParams* p = ps + s;
+    const uint32_t nreg = p->nreg;
+    if (nreg < 2) return;   // inactive streams have nreg 0
+    const uint32_t ntile = (nreg + kScanTile - 1) / kScanTile;
+    const uint32_t jobs = *(volatile uint32_t*) (p->scan_flags + ntile + 1);
+    const uint32_t want = min((jobs + kWalkThreads - 1) / kWalkThreads, walk_ctas_for(nreg));
+    if (!want) return;
+    const uint32_t at = atomicAdd(count, want);
+    for (uint32_t i = 0; i < want; ++i) list[at + i] = s;
+}
+
 __global__ void __launch_bounds__(kWalkThreads) k_wwalk_batch(const DecodeParams* ps,
-                                                              const BatchItem* items) {
+                                                              const uint32_t* list,
+                                                              uint32_t* count) {
     __shared__ DecodeParams sp;
-    const BatchItem it = items[blockIdx.x];
-    load_params(sp, ps + it.stream);
-    if (sp.cap_bytes) wwalk_body<true>(sp);
-    else wwalk_body<false>(sp);
+    __shared__ uint32_t s_item;
+    const uint32_t total = *(volatile uint32_t*) count;   // written by k_walk_items
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(count + 1, 1u);
+        __syncthreads();
+        const uint32_t it = s_item;
+        if (it >= total) return;
+        load_params(sp, ps + list[it]);
+        if (sp.cap_bytes) wwalk_body<true>(sp);
+        else wwalk_body<false>(sp);
+        __syncthreads();   // sp and s_item are rewritten next
+    }
 }
 
 // The batch ticket hands out items in list order; the list holds each
@@ -1903,6 +1947,8 @@ struct BatchLayout {
     size_t n_sync, n_walk, n_scan, n_final, n_items;
     bool any_capture;
     size_t smem_sync, smem_walk, smem_final, smem_prep;
+    size_t walk_list;     // [n_walk] stream of each merge-walk CTA (device-built)
+    uint32_t walk_grid;   // persistent merge-walk grid
 };
 
 static size_t stream_data_bytes(const BatchStreamPlan& sp) {
@@ -1916,6 +1962,8 @@ static uint32_t stage_cap_for(double per_unit, uint32_t B) {
     return (uint32_t) ((cap + 15) & ~(uint64_t) 15);
 }
 
+constexpr uint64_t kBatchRegionMax = 8192;   // units
+
 static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hint,
                       std::vector<BatchStreamPlan>& plans, BatchLayout& lay) {
     plans.assign(n, BatchStreamPlan{});
@@ -1923,6 +1971,15 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
     lay.n_sync = lay.n_walk = lay.n_scan = lay.n_final = 0;
     lay.any_capture = false;
     lay.smem_sync = lay.smem_walk = lay.smem_final = lay.smem_prep = 0;
+    // A batch finds its parallelism across streams: regions are sized so the
+    // whole batch gives about one G-pass wave of lanes (152 SMs x 16 warps),
+    // each with a similar number of symbols, but every stream keeps at least
+    // 32 regions, and never below the planner's length for the stream
+    // alone.  Longer regions mean fewer merge walks and fewer walks that
+    // cross a whole region.
+    double batch_sym = 0;
+    for (uint32_t i = 0; i < n; ++i) batch_sym += (double) d[i].n_out;
+    const double sym_per_lane = batch_sym / (152.0 * 16 * 32);
     for (uint32_t i = 0; i < n; ++i) {
         BatchStreamPlan& sp = plans[i];
         sp.active = d[i].n_out > 0;
@@ -1937,6 +1994,25 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
         h.flags |= d[i].flags & MANS_DECODE_NO_CAPTURE;
         int rc = mans_plan(d[i].n_units, d[i].n_out, d[i].L, &h, &sp.cfg);
         if (rc != MANS_OK) return rc;
+        if (h.region_blocks == 0) {
+            const double spu = (double) d[i].n_out / (double) d[i].n_units;
+            const uint64_t B = sp.cfg.block_units;
+            // at least a full warp (32 regions) per stream: a G-pass warp
+            // costs its issue slots however few of its lanes have a region
+            const uint64_t want = (uint64_t) std::min(
+                {sym_per_lane / std::max(spu, 1e-3), (double) d[i].n_units / kSyncThreads,
+                 (double) kBatchRegionMax});
+            const uint64_t cur = (uint64_t) sp.cfg.region_blocks * B;
+            if (want > cur) {
+                h.block_units = (uint32_t) B;
+                h.region_blocks =
+                    (uint32_t) std::max<uint64_t>(1, std::min<uint64_t>(want, d[i].n_units + B) / B) | 1u;
+                h.walk_slots = 0;
+                h.capture_bytes = 0;
+                rc = mans_plan(d[i].n_units, d[i].n_out, d[i].L, &h, &sp.cfg);
+                if (rc != MANS_OK) return rc;
+            }
+        }
         sp.cfg.flags = d[i].flags & MANS_DECODE_SOURCE_ORDER;
         sp.nblk = num_blocks(d[i].n_units, sp.cfg.block_units);
         sp.nreg = (sp.nblk + sp.cfg.region_blocks - 1) / sp.cfg.region_blocks;
@@ -1963,13 +2039,14 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
                                             ((size_t) 32 * tile_stride + 16 + sp.stage_cap + 16));
         lay.smem_prep = std::max(lay.smem_prep, (size_t) d[i].L * 12);
     }
-    lay.n_items = lay.n_sync + lay.n_walk + lay.n_scan + lay.n_final;
+    lay.n_items = lay.n_sync + lay.n_scan + lay.n_final;   // merge walks: built on the device
     size_t o = 0;
     lay.status = o; o += align256((size_t) n * 4);
     lay.flags = o; o += align256(flag_words * 4);
     lay.ticket = o; o += 256;
     lay.params = o; o += align256((size_t) n * sizeof(DecodeParams));
     lay.items = o; o += align256(lay.n_items * sizeof(BatchItem));
+    lay.walk_list = o; o += align256(lay.n_walk * 4);
     lay.data = o; o += data;
     lay.total = o;
     return MANS_OK;
@@ -2058,7 +2135,7 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
     b->slice.assign(n, nullptr);
     b->ps.assign(n, DecodeParams{});
     b->items.assign(b->lay.n_items, BatchItem{});
-    size_t is = 0, iw = b->lay.n_sync, ic = iw + b->lay.n_walk, iff = ic + b->lay.n_scan;
+    size_t is = 0, ic = b->lay.n_sync, iff = ic + b->lay.n_scan;
     for (uint32_t i = 0; i < n; ++i) {
         const BatchStreamPlan& sp = b->plans[i];
         DecodeParams& p = b->ps[i];
@@ -2102,7 +2179,6 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         p.cap_valid = sp.cfg.capture_bytes ? (uint32_t*) (slice + a.cap_valid) : nullptr;
         p.fb_list = sp.cfg.capture_bytes ? (uint32_t*) (slice + a.fb_list) : nullptr;
         for (size_t r = 0; r < sp.nreg; r += kSyncThreads) b->items[is++] = {i, (uint32_t) r, 0, 0};
-        for (uint32_t c = 0; c < walk_ctas(sp.nreg); ++c) b->items[iw++] = {i, c, 0, 0};
         for (size_t t = 0; t < sp.ntiles; ++t) b->items[ic++] = {i, (uint32_t) t, 0, 0};
         const uint32_t nctas = (uint32_t) ((sp.nblk + kFinalThreads - 1) / kFinalThreads);
         for (uint32_t c = 0; c < nctas; ++c) b->items[iff++] = {i, c, nctas, 0};
@@ -2125,6 +2201,19 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         return MANS_ERR_CUDA;
     }
     set_kernel_attributes();
+    if (b->lay.n_walk) {
+        // the persistent merge-walk grid: as many CTAs as stay resident
+        int per_sm = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_wwalk_batch, kWalkThreads,
+                                                          b->lay.smem_walk) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device) !=
+                cudaSuccess) {
+            mans_batch_destroy(b);
+            return MANS_ERR_CUDA;
+        }
+        b->lay.walk_grid = (uint32_t) std::min<size_t>(
+            b->lay.n_walk, (size_t) std::max(per_sm, 1) * (size_t) std::max(sms, 1));
+    }
     *out = b;
     return MANS_OK;
 }
@@ -2155,21 +2244,33 @@ int mans_batch_decode(mans_batch* b, void* stream) {
     if (L.n_items == 0) return MANS_OK;
     const DecodeParams* ps = (const DecodeParams*) (b->base + L.params);
     const BatchItem* items = (const BatchItem*) (b->base + L.items);
+    timing_mark(0, st);
     k_prep_batch<<<b->n, 1024, L.smem_prep, st>>>(ps);
+    timing_mark(1, st);
     if (L.n_sync)
         k_gwalk_batch<<<(unsigned) L.n_sync, kSyncThreads, L.smem_sync, st>>>(ps, items);
-    if (L.n_walk)
-        k_wwalk_batch<<<(unsigned) L.n_walk, kWalkThreads, L.smem_walk, st>>>(ps, items + L.n_sync);
+    timing_mark(2, st);
+    if (L.n_walk) {
+        // ticket words: 0 scan tiles, 1 merge-walk items, 2 next item
+        uint32_t* const count = (uint32_t*) (b->base + L.ticket) + 1;
+        uint32_t* const list = (uint32_t*) (b->base + L.walk_list);
+        k_walk_items<<<(b->n + 255) / 256, 256, 0, st>>>(ps, b->n, list, count);
+        k_wwalk_batch<<<L.walk_grid, kWalkThreads, L.smem_walk, st>>>(ps, list, count);
+    }
+    timing_mark(3, st);
     if (L.n_scan)
         k_scan_batch<<<(unsigned) L.n_scan, kScanThreads, 0, st>>>(
-            ps, items + L.n_sync + L.n_walk, (uint32_t*) (b->base + L.ticket));
+            ps, items + L.n_sync, (uint32_t*) (b->base + L.ticket));
+    timing_mark(4, st);
     if (L.n_final && L.any_capture)
         k_copy_batch<<<(unsigned) L.n_final, kCopyThreads, 0, st>>>(
-            ps, items + L.n_sync + L.n_walk + L.n_scan);
+            ps, items + L.n_sync + L.n_scan);
     if (L.n_final)
         k_final_batch<<<(unsigned) L.n_final, kFinalThreads, L.smem_final, st>>>(
-            ps, items + L.n_sync + L.n_walk + L.n_scan);
-    g_last_launches = 1 + (L.n_sync ? 1 : 0) + (L.n_walk ? 1 : 0) + (L.n_scan ? 1 : 0) +
+            ps, items + L.n_sync + L.n_scan);
+    timing_mark(5, st);
+    if (g_timing.on && g_timing.used < g_timing.cap) ++g_timing.used;
+    g_last_launches = 1 + (L.n_sync ? 1 : 0) + (L.n_walk ? 2 : 0) + (L.n_scan ? 1 : 0) +
                       (L.n_final ? (L.any_capture ? 2 : 1) : 0);
     return cudaGetLastError() == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
 }
