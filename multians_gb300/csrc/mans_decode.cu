@@ -1658,8 +1658,10 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
         uint64_t R = (n_units + lanes - 1) / lanes;
         R = std::min<uint64_t>(std::max<uint64_t>(R, std::max<uint64_t>(r_sync, 64)), r_max);
         // an odd block count keeps lanes of a warp (one region each) off
-        // power-of-two strides, which would pile them into the same L1 sets
-        c.region_blocks = (uint32_t) std::max<uint64_t>(8, R / c.block_units) | 1u;
+        // power-of-two strides, which would pile them into the same L1 sets;
+        // rounded up, so the regions never outnumber the lanes of one wave
+        c.region_blocks =
+            (uint32_t) std::max<uint64_t>(8, (R + c.block_units - 1) / c.block_units) | 1u;
     }
     if (c.walk_slots == 0) {
         const uint64_t R = (uint64_t) c.region_blocks * c.block_units;
