@@ -69,7 +69,7 @@ typedef struct {
 #define MANS_DECODE_SOURCE_ORDER 0x1u
 
 /* Symbol capture.  When the stream has at least two bits per symbol on
- * average (few zero-bit codewords), L <= 1024 and at least 16 Mi units (64
+ * average (few zero-bit codewords), L <= 4096 and at least 16 Mi units (64
  * MiB compressed; below that the capture's fixed cost outweighs what it
  * saves), or when capture_bytes is given, the planner gives every sync
  * region capture_bytes of workspace: the sync passes, which decode each

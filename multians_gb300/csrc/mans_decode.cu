@@ -1487,6 +1487,23 @@ static size_t sync_smem(uint32_t L, uint32_t threads, bool capture) {
            (threads / 32) * 40 + (capture ? 4096 + (size_t) (threads / 32) * kCapWarpBytes : 0);
 }
 
+// Resident lanes of a capturing G pass with `threads`-thread CTAs: shared
+// memory bounds it (228 KB per SM, 1 KB of it reserved per CTA).
+static uint64_t capture_lanes(uint32_t L, uint32_t threads) {
+    const uint64_t per_sm = std::min<uint64_t>(233472 / (sync_smem(L, threads, true) + 1024),
+                                               2048 / threads);
+    return 152ull * std::max<uint64_t>(per_sm, 1) * threads;
+}
+
+// CTA size of a capturing G pass over nreg regions: 128 threads (finer
+// balance over the SMs) while their resident lanes hold the regions in one
+// wave or outnumber those of 256-thread CTAs, else 256.
+static uint32_t capture_threads(uint32_t L, size_t nreg) {
+    const uint64_t small = capture_lanes(L, kSyncThreads);
+    const uint64_t big = capture_lanes(L, kSyncThreadsMax);
+    return (nreg <= small || small >= big) ? kSyncThreads : kSyncThreadsMax;
+}
+
 static size_t walk_smem(uint32_t L, bool capture) {
     return (((size_t) L * 8 + 15) & ~(size_t) 15) + (size_t) kWalkThreads * kWindowStride +
            (kWalkThreads / 32) * 8 + (capture ? 16 + (kWalkThreads / 32) * kCapWarpBytes : 0);
@@ -1611,7 +1628,7 @@ static double mean_meeting_units(uint32_t L, double bits_per_symbol) {
 // and saves the final pass time in proportion to the output (0.8 us per
 // MiB at 6 bits per symbol): from 16 M units on it pays.
 constexpr double kCaptureMinBits = 2.0;
-constexpr uint32_t kCaptureMaxL = 1024;   // larger tables leave too little shared memory
+constexpr uint32_t kCaptureMaxL = 4096;   // larger tables leave too little shared memory
 constexpr size_t kCaptureMinUnits = 16u << 20;
 
 int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
@@ -1647,14 +1664,18 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
     // three mean meeting distances and 512 units (2048 for L > 1024; more
     // when three meeting distances are longer): measured over 0.67 .. 8.6
     // bits per symbol and L = 1024 / 4096, between about 2.5 and 4 meeting
-    // distances is best.  With capture the G pass holds 16 warps per SM,
-    // so R may grow to 1024 units to keep that one wave.
+    // distances is best.  With capture the lanes are those the capturing G
+    // pass keeps resident (16 warps per SM at L = 1024, 8 at L = 2048 and
+    // 4096: the rings and the table fill shared memory), and R may grow to
+    // 4096 units to keep them one wave.
     const uint64_t tail = std::max<uint64_t>(256, 4ull * L);
     const double meet = mean_meeting_units(L, bps);
     if (c.region_blocks == 0) {
-        const uint64_t lanes = 152ull * 16 * 32;
+        const uint64_t lanes =
+            capture ? std::max(capture_lanes(L, kSyncThreads), capture_lanes(L, kSyncThreadsMax))
+                    : 152ull * 16 * 32;
         const uint64_t r_sync = (uint64_t) (3.0 * meet);
-        const uint64_t r_max = std::max<uint64_t>(capture ? 1024 : (L <= 1024 ? 512 : 2048), r_sync);
+        const uint64_t r_max = std::max<uint64_t>(capture ? 4096 : (L <= 1024 ? 512 : 2048), r_sync);
         uint64_t R = (n_units + lanes - 1) / lanes;
         R = std::min<uint64_t>(std::max<uint64_t>(R, std::max<uint64_t>(r_sync, 64)), r_max);
         // an odd block count keeps lanes of a warp (one region each) off
@@ -1782,12 +1803,10 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     uint64_t cap = (uint64_t) (per_unit * 32.0 * cfg.block_units * 1.5) + 256;
     cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
     p.stage_cap = (uint32_t) ((cap + 15) & ~(uint64_t) 15);
-    // G-pass CTAs: 256 threads share a table for L >= 4096; with capture 128
-    // (three CTAs, 12 warps per SM) while the regions fit that in one wave,
-    // else 256 (two CTAs, 16 warps)
+    // G-pass CTAs: 256 threads share a table for L >= 4096; with capture as
+    // capture_threads picks
     const uint32_t gthreads =
-        capture ? (nreg <= 152ull * 3 * kSyncThreads ? kSyncThreads : kSyncThreadsMax)
-                : (L >= 4096 ? kSyncThreadsMax : kSyncThreads);
+        capture ? capture_threads(L, nreg) : (L >= 4096 ? kSyncThreadsMax : kSyncThreads);
     const size_t smem_sync = sync_smem(L, gthreads, capture);
     const size_t smem_walk = walk_smem(L, capture);
     const uint32_t tile_bytes = (cfg.block_units + 4) * 4;

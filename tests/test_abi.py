@@ -52,14 +52,14 @@ def test_plan_and_aux_sizes(mg):
     need = mg.aux_size(50_000_000, p)
     assert 0 < need <= mg.aux_size_max(50_000_000)
     small = mg.plan(1000, 5000, 4096)
-    assert small["capture_bytes"] == 0   # 6.4 bits/symbol but L > 1024
+    assert small["capture_bytes"] == 0   # too short
     assert mg.aux_size(1000, small) <= mg.aux_size_max(1000)
 
 
 def test_capture_plan(mg):
     """6 bits per symbol at L = 1024 captures: one slice per region holding
     the region's symbols and a walk's with room to spare; low-entropy
-    streams and L > 1024 do not."""
+    streams, short ones and L > 4096 do not."""
     n_units, n_out = 50_000_000, 268_435_456
     p = mg.plan(n_units, n_out, 1024)
     R = p["block_units"] * p["region_blocks"]
@@ -71,7 +71,9 @@ def test_capture_plan(mg):
     extra = mg.aux_size(n_units, p) - mg.aux_size(n_units, dict(p, capture_bytes=0))
     assert extra >= nreg * p["capture_bytes"]
     assert mg.plan(20_000_000, 400_000_000, 1024)["capture_bytes"] == 0   # 1.6 bits/symbol
-    assert mg.plan(20_000_000, 100_000_000, 4096)["capture_bytes"] == 0
+    assert mg.plan(20_000_000, 100_000_000, 8192)["capture_bytes"] == 0
+    p4 = mg.plan(20_000_000, 100_000_000, 4096)   # L = 4096: half the resident lanes
+    assert p4["capture_bytes"] > 0
     assert mg.plan(12_000_000, 64_000_000, 1024)["capture_bytes"] == 0    # short stream
     forced = mg.plan(1_000_000, 20_000_000, 1024, {"capture_bytes": 1000})
     assert forced["capture_bytes"] == 1008
