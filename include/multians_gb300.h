@@ -79,6 +79,10 @@ typedef struct {
  * turns this off (smaller workspace, every block decoded in the final
  * pass); the output is identical either way. */
 #define MANS_DECODE_NO_CAPTURE 0x2u
+/* Capture whenever bits per symbol and L allow it, whatever the stream's
+ * length (measured on the 4096-stream batch workload, where every stream is
+ * short, capture lost: the capturing G pass holds fewer warps per SM). */
+#define MANS_DECODE_CAPTURE 0x4u
 
 /* Fills `out` with the geometry the decoder uses for this call. */
 int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,

@@ -18,6 +18,7 @@ from ._lib import (  # noqa: F401
     DEV_COUNT_MISMATCH,
     DECODE_SOURCE_ORDER,
     DECODE_NO_CAPTURE,
+    DECODE_CAPTURE,
     lib,
     plan,
     aux_size,

@@ -39,6 +39,7 @@ class MansError(RuntimeError):
 
 DECODE_SOURCE_ORDER = 0x1
 DECODE_NO_CAPTURE = 0x2
+DECODE_CAPTURE = 0x4
 
 
 class Cfg(ctypes.Structure):

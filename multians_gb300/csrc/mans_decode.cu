@@ -1641,7 +1641,7 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
     const bool capture = !(c.flags & MANS_DECODE_NO_CAPTURE) &&
                          (c.capture_bytes != 0 ||
                           (n_out > 0 && L <= kCaptureMaxL && bps >= kCaptureMinBits &&
-                           n_units >= kCaptureMinUnits));
+                           (n_units >= kCaptureMinUnits || (c.flags & MANS_DECODE_CAPTURE))));
     if (!capture) c.capture_bytes = 0;
     if (c.block_units == 0) {
         // about 128 symbols per block
@@ -2012,7 +2012,7 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
             return MANS_ERR_ARG;
         mans_cfg h = {0, 0, 0, 0, 0, 0};
         if (hint) h = *hint;
-        h.flags |= d[i].flags & MANS_DECODE_NO_CAPTURE;
+        h.flags |= d[i].flags & (MANS_DECODE_NO_CAPTURE | MANS_DECODE_CAPTURE);
         int rc = mans_plan(d[i].n_units, d[i].n_out, d[i].L, &h, &sp.cfg);
         if (rc != MANS_OK) return rc;
         if (h.region_blocks == 0) {

@@ -77,6 +77,9 @@ def test_capture_plan(mg):
     assert mg.plan(12_000_000, 64_000_000, 1024)["capture_bytes"] == 0    # short stream
     forced = mg.plan(1_000_000, 20_000_000, 1024, {"capture_bytes": 1000})
     assert forced["capture_bytes"] == 1008
+    short = mg.plan(1_000_000, 5_000_000, 1024, {"flags": mg.DECODE_CAPTURE})
+    assert short["capture_bytes"] > 0                                      # asked for
+    assert mg.plan(1_000_000, 20_000_000, 1024, {"flags": mg.DECODE_CAPTURE})["capture_bytes"] == 0
 
 
 def test_table_check(mg, oracle_lib):
