@@ -124,6 +124,21 @@ int mans_decode_sync(const uint32_t* d_units, size_t n_units,
                      void* d_aux, size_t aux_bytes, const mans_cfg* hint,
                      void* stream, uint32_t* status_out);
 
+/* Workspace and table management for callers that do not hold device
+ * memory of their own (the reference's CUHDGPUDecoderMemory::allocate /
+ * free, src/multians_gpu_decoder_memory.cc:21-50, and
+ * CUHDGPUCodetable's cpy_host_to_device, include/cuhd_gpu_memory_buffer.hxx:
+ * 36-61).  mans_aux_alloc plans the decode of (n_units, n_out, L) (hint may
+ * be NULL) and allocates exactly the workspace that plan needs, symbol
+ * capture included; *bytes receives its size.  mans_table_upload checks a
+ * host table (mans_table_check) and copies it to new device memory;
+ * single-symbol tables are accepted (the decode fills the output). */
+int mans_aux_alloc(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
+                   void** d_aux, size_t* bytes);
+int mans_aux_free(void* d_aux);
+int mans_table_upload(const uint32_t* h_table, uint32_t L, uint32_t** d_table);
+int mans_table_free(uint32_t* d_table);
+
 /* Host-side table check: 0 if every entry decodes inside [L, 2L) and
  * zero-bit entries strictly decrease the state, 1 if the table holds a
  * single symbol (all entries are zero-bit self loops), -1 otherwise. */
@@ -192,6 +207,14 @@ int mans_batch_status(mans_batch* b, void* stream, uint32_t* or_status, uint32_t
  * workspace slice, and updates its status.  Allocates nothing. */
 int mans_batch_fixup(mans_batch* b, void* stream, uint32_t* n_redone);
 int mans_batch_destroy(mans_batch* b);
+
+/* One call for a batch: plan, decode (in d_workspace when given, else in
+ * memory it allocates and frees), wait, re-decode streams whose walks ran
+ * out of slots, and report the OR of the device status bits (and, if
+ * per_stream != NULL, each stream's).  Synchronous on `stream`. */
+int mans_decode_batch(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                      void* d_workspace, size_t workspace_bytes, void* stream,
+                      uint32_t* or_status, uint32_t* per_stream);
 
 /* Serving loop.  No counterpart in the reference, whose decode is one
  * blocking call on the default stream (include/cuhd_gpu_decoder.h:22-36).

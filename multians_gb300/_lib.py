@@ -72,6 +72,11 @@ SIGNATURES = {
                                            ctypes.POINTER(ctypes.c_int)]),
     "mans_decode_sync": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _u32, _u32, _u32, _vp, _sz,
                                         ctypes.POINTER(Cfg), _vp, _u32p]),
+    "mans_aux_alloc": (ctypes.c_int, [_sz, _sz, _u32, ctypes.POINTER(Cfg),
+                                      ctypes.POINTER(_vp), ctypes.POINTER(_sz)]),
+    "mans_aux_free": (ctypes.c_int, [_vp]),
+    "mans_table_upload": (ctypes.c_int, [_u32p, _u32, ctypes.POINTER(_vp)]),
+    "mans_table_free": (ctypes.c_int, [_vp]),
 }
 
 _lib = None

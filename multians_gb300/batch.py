@@ -33,6 +33,9 @@ def _sig():
     L.mans_batch_status.restype = ctypes.c_int
     L.mans_batch_fixup.argtypes = [vp, vp, ctypes.POINTER(u32)]
     L.mans_batch_fixup.restype = ctypes.c_int
+    L.mans_decode_batch.argtypes = [ctypes.POINTER(StreamDesc), u32, ctypes.POINTER(Cfg), vp,
+                                    ctypes.c_size_t, vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    L.mans_decode_batch.restype = ctypes.c_int
     L.mans_batch_destroy.argtypes = [vp]
     L.mans_batch_destroy.restype = ctypes.c_int
     return L
@@ -110,3 +113,20 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def decode_batch(descs, hint: dict | None = None, workspace=None, stream=None):
+    """One synchronous call for a batch (mans_decode_batch): returns the OR
+    of the device status bits and each stream's."""
+    L = _sig()
+    n = len(descs)
+    arr = (StreamDesc * n)(*descs)
+    h = Cfg(**hint) if hint else None
+    acc = ctypes.c_uint32(0)
+    per = (ctypes.c_uint32 * n)()
+    ws_ptr = ctypes.c_void_p(workspace.data_ptr()) if workspace is not None else None
+    ws_bytes = workspace.numel() if workspace is not None else 0
+    st = ctypes.c_void_p(stream.cuda_stream) if stream is not None else None
+    check(L.mans_decode_batch(arr, n, ctypes.byref(h) if h else None, ws_ptr, ws_bytes, st,
+                              ctypes.byref(acc), per), "mans_decode_batch")
+    return int(acc.value), [int(x) for x in per]

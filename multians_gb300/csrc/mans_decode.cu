@@ -1899,6 +1899,51 @@ int mans_aux_status(const void* d_aux, void* stream, uint32_t* status_out) {
     return MANS_OK;
 }
 
+int mans_aux_alloc(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
+                   void** d_aux, size_t* bytes) {
+    if (!d_aux || !bytes) return MANS_ERR_ARG;
+    *d_aux = nullptr;
+    *bytes = 0;
+    mans_cfg plan;
+    const int rc = mans_plan(n_units ? n_units : 1, n_out, L, hint, &plan);
+    if (rc != MANS_OK) return rc;
+    const size_t need = mans_aux_size(n_units ? n_units : 1, &plan);
+    if (cudaMalloc(d_aux, need) != cudaSuccess) {
+        cudaGetLastError();
+        *d_aux = nullptr;
+        return MANS_ERR_NOMEM;
+    }
+    *bytes = need;
+    return MANS_OK;
+}
+
+int mans_aux_free(void* d_aux) {
+    if (!d_aux) return MANS_OK;
+    return cudaFree(d_aux) == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
+}
+
+int mans_table_upload(const uint32_t* h_table, uint32_t L, uint32_t** d_table) {
+    if (!h_table || !d_table || L < 2 || L > kMaxStates) return MANS_ERR_ARG;
+    *d_table = nullptr;
+    if (mans_table_check(h_table, L) < 0) return MANS_ERR_TABLE;
+    void* p = nullptr;
+    if (cudaMalloc(&p, (size_t) L * 4) != cudaSuccess) {
+        cudaGetLastError();
+        return MANS_ERR_NOMEM;
+    }
+    if (cudaMemcpy(p, h_table, (size_t) L * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(p);
+        return MANS_ERR_CUDA;
+    }
+    *d_table = (uint32_t*) p;
+    return MANS_OK;
+}
+
+int mans_table_free(uint32_t* d_table) {
+    if (!d_table) return MANS_OK;
+    return cudaFree(d_table) == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
+}
+
 int mans_status_code(uint32_t st) {
     if (st & MANS_DEV_BAD_TABLE) return MANS_ERR_TABLE;
     if (st & (MANS_DEV_SYNC_OVERFLOW | MANS_DEV_COUNT_MISMATCH)) return MANS_ERR_SYNC;
@@ -2355,6 +2400,24 @@ int mans_batch_fixup(mans_batch* b, void* stream, uint32_t* n_redone) {
         if (n_redone) ++*n_redone;
     }
     return MANS_OK;
+}
+
+int mans_decode_batch(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hint,
+                      void* d_workspace, size_t workspace_bytes, void* stream,
+                      uint32_t* or_status, uint32_t* per_stream) {
+    if (or_status) *or_status = 0;
+    mans_batch* b = nullptr;
+    int rc = mans_batch_create(streams, n, hint, d_workspace, workspace_bytes, &b);
+    if (rc != MANS_OK) return rc;
+    uint32_t acc = 0, redone = 0;
+    rc = mans_batch_decode(b, stream);
+    if (rc == MANS_OK) rc = mans_batch_status(b, stream, &acc, nullptr);
+    if (rc == MANS_OK && (acc & MANS_DEV_SYNC_OVERFLOW)) rc = mans_batch_fixup(b, stream, &redone);
+    if (rc == MANS_OK) rc = mans_batch_status(b, stream, &acc, per_stream);
+    mans_batch_destroy(b);
+    if (rc != MANS_OK) return rc;
+    if (or_status) *or_status = acc;
+    return mans_status_code(acc & ~MANS_DEV_DEGENERATE);
 }
 
 int mans_batch_status(mans_batch* b, void* stream, uint32_t* or_status, uint32_t* per_stream) {

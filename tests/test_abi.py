@@ -109,3 +109,18 @@ def test_decode_rejects_bad_arguments_without_gpu(mg):
     rc = lib.mans_decode(dummy, 1000, dummy, 1000, dummy, 1024, 1024, 0, dummy, 8,
                          ctypes.byref(c), None)
     assert rc == mg.Status.ERR_AUX_SMALL
+
+
+def test_table_upload_rejects_bad_tables(mg, oracle_lib):
+    """mans_table_upload checks the table on the host before touching the
+    device: bad tables and bad arguments fail without a GPU."""
+    import ctypes
+    st = oracle_lib.make_stream(seed=3, lam=0.05, n=5000, L=1024)
+    bad = np.ascontiguousarray(st.table, dtype=np.uint32).copy()
+    bad[3] = (bad[3] & 0x00FFFFFF) | (20 << 24)
+    out = ctypes.c_void_p()
+    p = bad.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+    assert mg.lib().mans_table_upload(p, 1024, ctypes.byref(out)) == mg.Status.ERR_TABLE
+    assert mg.lib().mans_table_upload(p, 1, ctypes.byref(out)) == mg.Status.ERR_ARG
+    assert mg.lib().mans_table_upload(None, 1024, ctypes.byref(out)) == mg.Status.ERR_ARG
+    assert mg.lib().mans_aux_free(None) == 0 and mg.lib().mans_table_free(None) == 0
