@@ -146,13 +146,71 @@ def run_batched(args, ws, rank, local):
         e1.record(stream)
         torch.cuda.synchronize(dev)
         e2e_times.append(e0.elapsed_time(e1))
-    e2e_ms = sorted(e2e_times)[1]
+    e2e_serial_ms = sorted(e2e_times)[1]
     if n_overflow:
         b.fixup(stream)
         h_out_all.copy_(d_out_all)
     ho_np = h_out_all.numpy()
     e2e_ok = all(np.array_equal(ho_np[oo[i]: oo[i + 1]][::-1], st.symbols)
                  for i, st in enumerate(sts))
+
+    # pipelined e2e, as a streaming caller runs it: a second buffer set and
+    # batch; step i's input copy, decode and output copy on three streams,
+    # each waiting only on what it reads or overwrites (the decode of step
+    # i overlaps the input copy of step i+1 and the output copy of step
+    # i-1); every step still moves all its bytes
+    e2e_ms = e2e_serial_ms
+    pipelined = n_overflow == 0
+    if pipelined:
+        d_units2 = torch.empty_like(d_units_all)
+        d_out2 = torch.empty_like(d_out_all)
+        h_out2 = torch.empty_like(h_out_all).pin_memory()
+        units2 = [d_units2[int(offs[i]): int(offs[i]) + st.units.size] for i, st in enumerate(sts)]
+        outs2 = [d_out2[int(oo[i]): int(oo[i + 1])] for i in range(len(sts))]
+        descs2 = [batch.desc(u, st.n_units, o, st.n, t, st.L, st.first_state, st.first_bit,
+                             capture=cap) for st, u, t, o in zip(sts, units2, tables, outs2)]
+        b2 = batch.Batch(descs2)
+        b2.graph_decode(stream)
+        sets = [(d_units_all, d_out_all, h_out_all, b), (d_units2, d_out2, h_out2, b2)]
+        s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+        def run(nsteps):
+            ev = lambda: torch.cuda.Event()  # noqa: E731
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            in_done, dec_done, out_done = [], [], []
+            t0.record(s_in)
+            for i in range(nsteps):
+                du, do, ho, bb = sets[i & 1]
+                with torch.cuda.stream(s_in):
+                    if i >= 2:
+                        s_in.wait_event(dec_done[i - 2])
+                    du.copy_(h_units_all, non_blocking=True)
+                    in_done.append(ev())
+                    in_done[i].record(s_in)
+                stream.wait_event(in_done[i])
+                if i >= 2:
+                    stream.wait_event(out_done[i - 2])
+                bb.graph_decode(stream)
+                dec_done.append(ev())
+                dec_done[i].record(stream)
+                s_out.wait_event(dec_done[i])
+                with torch.cuda.stream(s_out):
+                    ho.copy_(do, non_blocking=True)
+                    out_done.append(ev())
+                    out_done[i].record(s_out)
+            t1.record(s_out)
+            torch.cuda.synchronize(dev)
+            return t0.elapsed_time(t1) / nsteps, (nsteps - 1) & 1
+
+        run(2)
+        e2e_ms, last = run(6)
+        acc2, _ = sets[last][3].status(stream)
+        hl = sets[last][2].numpy()
+        e2e_ok = e2e_ok and (acc2 & ~mg.DEV_DEGENERATE) == 0 and all(
+            np.array_equal(hl[oo[i]: oo[i + 1]][::-1], st.symbols) for i, st in enumerate(sts))
+        b2.close()
+        del d_units2, d_out2, h_out2
     b.close()
     if rank != 0:
         return
@@ -184,7 +242,10 @@ def run_batched(args, ws, rank, local):
         "cpu_baseline": None,
         "e2e": {"value": round(ws * total_sym / (e2e_ms / 1e3) / 1e9, 3), "unit": "GB/s",
                 "h2d_bytes_per_step": int(offs[-1]) * 4, "d2h_bytes_per_step": total_sym,
-                "bit_exact": bool(e2e_ok)},
+                "bit_exact": bool(e2e_ok),
+                "pipelined": "2 buffer sets and batches; H2D, graph decode, D2H on 3 streams"
+                if pipelined else None,
+                "serial_value": round(ws * total_sym / (e2e_serial_ms / 1e3) / 1e9, 3)},
         "gpu_launches": 4 * steps,
         "clocks": clk.summary(),
         "gen_seconds": round(gen_s, 2),
