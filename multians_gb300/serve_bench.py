@@ -157,7 +157,8 @@ def run(args, ws, rank, local):
     h_units = [torch.from_numpy(st.units.view(np.int32)).pin_memory() for st in sts]
     h_out = [torch.empty(max(1, st.n), dtype=torch.uint8).pin_memory() for st in sts]
 
-    srv = serve.Server(budget_bytes=budget)
+    inflight = int(os.environ.get("MANS_SERVE_INFLIGHT", "0"))   # 0: the library default
+    srv = serve.Server(budget_bytes=budget, max_inflight=inflight)
     tids = [srv.add_table(st.table) for st in sts]
     cap = not getattr(args, "no_capture", False)
     rp_dev = Replay(serve, entry, [t.data_ptr() for t in d_units], [t.data_ptr() for t in d_out],
