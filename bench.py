@@ -306,16 +306,19 @@ def run_ours(args, ws, rank, local):
         one()
         out_h.copy_(out, non_blocking=True)
     torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(e2e_steps):
-        units.copy_(units_h, non_blocking=True)
-        table.copy_(table_h, non_blocking=True)
-        one()
-        out_h.copy_(out, non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    e2e_serial_ms = e0.elapsed_time(e1) / e2e_steps
+    serial_runs = []
+    for _ in range(3):   # median of three runs: the host links are shared with other GPUs
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(e2e_steps):
+            units.copy_(units_h, non_blocking=True)
+            table.copy_(table_h, non_blocking=True)
+            one()
+            out_h.copy_(out, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        serial_runs.append(e0.elapsed_time(e1) / e2e_steps)
+    e2e_serial_ms = statistics.median(serial_runs)
     e2e_ok = bool(np.array_equal(out_h.numpy(), st.symbols[::-1]))
 
     units2 = [units, torch.empty_like(units)]
@@ -356,7 +359,9 @@ def run_ours(args, ws, rank, local):
         return t0.elapsed_time(t1) / steps, (steps - 1) & 1
 
     pipelined(2)
-    e2e_ms, last = pipelined(e2e_steps)
+    runs = [pipelined(e2e_steps) for _ in range(3)]
+    e2e_ms = statistics.median(r[0] for r in runs)
+    last = runs[-1][1]
     e2e_ok = e2e_ok and bool(np.array_equal(out_h2[last].numpy(), st.symbols[::-1]))
     e2e_ok = e2e_ok and aux_status(aux, stream) == 0
     del units2, table2, out2, out_h2

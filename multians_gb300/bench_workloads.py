@@ -204,7 +204,9 @@ def run_batched(args, ws, rank, local):
             return t0.elapsed_time(t1) / nsteps, (nsteps - 1) & 1
 
         run(2)
-        e2e_ms, last = run(6)
+        runs = [run(6) for _ in range(3)]   # median: the host links are shared
+        e2e_ms = sorted(r[0] for r in runs)[1]
+        last = runs[-1][1]
         acc2, _ = sets[last][3].status(stream)
         hl = sets[last][2].numpy()
         e2e_ok = e2e_ok and (acc2 & ~mg.DEV_DEGENERATE) == 0 and all(
