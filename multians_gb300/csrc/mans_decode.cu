@@ -2244,9 +2244,27 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         p.cap = sp.cfg.capture_bytes ? (uint8_t*) (slice + a.cap) : nullptr;
         p.cap_valid = sp.cfg.capture_bytes ? (uint32_t*) (slice + a.cap_valid) : nullptr;
         p.fb_list = sp.cfg.capture_bytes ? (uint32_t*) (slice + a.fb_list) : nullptr;
-        for (size_t r = 0; r < sp.nreg; r += kSyncThreads) b->items[is++] = {i, (uint32_t) r, 0, 0};
         for (size_t t = 0; t < sp.ntiles; ++t) b->items[ic++] = {i, (uint32_t) t, 0, 0};
-        const uint32_t nctas = (uint32_t) ((sp.nblk + kFinalThreads - 1) / kFinalThreads);
+    }
+    // G-pass and final-pass items, heaviest first: a batch's CTAs run in
+    // several waves (every stream has at least one CTA), and with the long
+    // ones issued first the short ones fill in behind them instead of a
+    // late long CTA setting the launch's end (longest-processing-time order)
+    std::vector<uint32_t> order;
+    for (uint32_t i = 0; i < n; ++i)
+        if (b->plans[i].active) order.push_back(i);
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        return (double) streams[x].n_out / (double) b->plans[x].nreg >
+               (double) streams[y].n_out / (double) b->plans[y].nreg;   // symbols per region
+    });
+    for (const uint32_t i : order)
+        for (size_t r = 0; r < b->plans[i].nreg; r += kSyncThreads)
+            b->items[is++] = {i, (uint32_t) r, 0, 0};
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        return streams[x].n_out > streams[y].n_out;
+    });
+    for (const uint32_t i : order) {
+        const uint32_t nctas = (uint32_t) ((b->plans[i].nblk + kFinalThreads - 1) / kFinalThreads);
         for (uint32_t c = 0; c < nctas; ++c) b->items[iff++] = {i, c, nctas, 0};
     }
     const size_t pbytes = n * sizeof(DecodeParams), ibytes = b->items.size() * sizeof(BatchItem);
