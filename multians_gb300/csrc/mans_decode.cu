@@ -1325,7 +1325,23 @@ __global__ void __launch_bounds__(kFinalThreads) k_final_fb(DecodeParams p) {
 
 template <bool kRev>
 __global__ void __launch_bounds__(kFinalThreads) k_final(DecodeParams p) {
-    final_body<kRev>(p, blockIdx.x, gridDim.x);
+    // persistent: the table is loaded once per CTA, then every warp takes
+    // every (grid x 8)-th group of 32 blocks
+    extern __shared__ __align__(16) uint2 s_tab[];
+    if (!final_prologue(p, blockIdx.x, gridDim.x, true)) return;
+    const uint32_t tb = smem_addr(s_tab);
+    const uint32_t warp = threadIdx.x >> 5, wpc = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        mbar_init(final_bar(p, tb, warp), 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    const uint32_t ngroups = (p.nblk + 31) >> 5;
+    uint32_t phase = 0;
+    for (uint32_t g = blockIdx.x * wpc + warp; g < ngroups; g += gridDim.x * wpc) {
+        if (!final_warp<kRev>(p, tb, g << 5, phase)) return;
+        phase ^= 1u;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1843,10 +1859,18 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
             k_final_fb<false><<<gfb, kFinalThreads, smem_final, st>>>(p);
         }
         ++launches;
-    } else if (rev) {
-        k_final<true><<<gf, kFinalThreads, smem_final, st>>>(p);
     } else {
-        k_final<false><<<gf, kFinalThreads, smem_final, st>>>(p);
+        // persistent final pass: as many CTAs as stay resident
+        int per_sm = 0, sms = 152, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &per_sm, rev ? k_final<true> : k_final<false>, kFinalThreads, smem_final) !=
+                cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        const unsigned gp = std::min<unsigned>(gf, (unsigned) (per_sm * std::max(sms, 1)));
+        if (rev) k_final<true><<<gp, kFinalThreads, smem_final, st>>>(p);
+        else k_final<false><<<gp, kFinalThreads, smem_final, st>>>(p);
     }
     timing_mark(5, st);
     if (g_timing.on && g_timing.used < g_timing.cap) ++g_timing.used;
