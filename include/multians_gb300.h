@@ -94,7 +94,10 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
 size_t mans_aux_size(size_t n_units, const mans_cfg* cfg);
 
 /* Worst-case aux bytes over every geometry mans_plan can pick for n_units
- * units (what CUHDGPUDecoderMemory::allocate reserves). */
+ * units without symbol capture (what CUHDGPUDecoderMemory::allocate
+ * reserves).  A decode given this much always runs: when the plan's capture
+ * does not fit it decodes without (capture slices scale with the output
+ * size, which this call does not see). */
 size_t mans_aux_size_max(size_t n_units);
 
 /* Decodes one stream; asynchronous on `stream`.  Replaces

@@ -1766,6 +1766,16 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     mans_cfg cfg;
     int rc = mans_plan(n_units, n_out, L, cfg_in, &cfg);
     if (rc != MANS_OK) return rc;
+    if (cfg.capture_bytes && !(cfg_in && cfg_in->capture_bytes) &&
+        mans_aux_size(n_units, &cfg) > aux_bytes) {
+        // capture was the planner's choice and does not fit: decode without
+        // it (a workspace of mans_aux_size_max bytes always suffices then)
+        mans_cfg h = cfg_in ? *cfg_in : mans_cfg{0, 0, 0, 0, 0, 0};
+        h.flags |= MANS_DECODE_NO_CAPTURE;
+        h.capture_bytes = 0;
+        rc = mans_plan(n_units, n_out, L, &h, &cfg);
+        if (rc != MANS_OK) return rc;
+    }
     const size_t nblk = num_blocks(n_units, cfg.block_units);
     const size_t nreg = (nblk + cfg.region_blocks - 1) / cfg.region_blocks;
     const AuxLayout lay = layout_for(nblk, nreg, cfg.walk_slots, cfg.capture_bytes);

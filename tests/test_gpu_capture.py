@@ -160,3 +160,17 @@ def test_default_capture_large_stream(mg):
     got = mg.decode(_dev(st.units), st.n_units, st.n, _dev(st.table), st.first_state,
                     st.first_bit, L=st.L, source_order=True).cpu().numpy()
     assert np.array_equal(got, st.symbols)
+    # a workspace with no room for the capture the planner picks (the size
+    # of the plan without it) still decodes: without capture
+    import torch
+
+    from multians_gb300.decoder import aux_status, decode_async
+    small = mg.aux_size(st.n_units, mg.plan(st.n_units, st.n, st.L,
+                                             {"flags": mg.DECODE_NO_CAPTURE}))
+    assert small < mg.aux_size(st.n_units, p) and small <= mg.aux_size_max(st.n_units)
+    aux = torch.empty(small, dtype=torch.uint8, device="cuda")
+    out = torch.full((st.n,), 0xAB, dtype=torch.uint8, device="cuda")
+    decode_async(_dev(st.units), st.n_units, out, st.n, _dev(st.table), st.L, st.first_state,
+                 st.first_bit, aux, {})
+    assert aux_status(aux) == 0
+    assert np.array_equal(out.cpu().numpy()[::-1], st.symbols)
