@@ -1824,9 +1824,11 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
         return MANS_ERR_CUDA;
     const size_t smem = ((size_t) L * sizeof(uint2) + 15) & ~(size_t) 15;
     set_kernel_attributes();
-    // staging per warp: 1.5x the expected symbols of 32 blocks, 16 B rounded
+    // staging per warp: 1.25x the expected symbols of 32 blocks, 16 B
+    // rounded (a warp whose range does not fit writes it directly, byte by
+    // byte; 1.5x put the batched final pass at two CTAs per SM)
     const double per_unit = (double) n_out / (double) n_units;
-    uint64_t cap = (uint64_t) (per_unit * 32.0 * cfg.block_units * 1.5) + 256;
+    uint64_t cap = (uint64_t) (per_unit * 32.0 * cfg.block_units * 1.25) + 128;
     cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
     p.stage_cap = (uint32_t) ((cap + 15) & ~(uint64_t) 15);
     // G-pass CTAs: 256 threads share a table for L >= 4096; with capture as
@@ -2057,7 +2059,7 @@ static size_t stream_data_bytes(const BatchStreamPlan& sp) {
 }
 
 static uint32_t stage_cap_for(double per_unit, uint32_t B) {
-    uint64_t cap = (uint64_t) (per_unit * 32.0 * B * 1.5) + 256;
+    uint64_t cap = (uint64_t) (per_unit * 32.0 * B * 1.25) + 128;
     cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
     return (uint32_t) ((cap + 15) & ~(uint64_t) 15);
 }
