@@ -1323,10 +1323,14 @@ __global__ void __launch_bounds__(kFinalThreads) k_final_fb(DecodeParams p) {
     final_fb_body<kRev>(p, blockIdx.x, gridDim.x);
 }
 
+// Plain decodes run k_final with 256 threads, or 384 for L >= 4096 (one
+// table per 12 warps: with a 32 KB table two CTAs fit an SM either way).
+constexpr uint32_t kFinalThreadsWide = 384;
+
 template <bool kRev>
-__global__ void __launch_bounds__(kFinalThreads) k_final(DecodeParams p) {
+__global__ void __launch_bounds__(kFinalThreadsWide) k_final(DecodeParams p) {
     // persistent: the table is loaded once per CTA, then every warp takes
-    // every (grid x 8)-th group of 32 blocks
+    // every (grid x warps)-th group of 32 blocks
     extern __shared__ __align__(16) uint2 s_tab[];
     if (!final_prologue(p, blockIdx.x, gridDim.x, true)) return;
     const uint32_t tb = smem_addr(s_tab);
@@ -1841,6 +1845,8 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
     const size_t per_warp_final = (size_t) 32 * tile_stride + 16 + p.stage_cap + 16;
     const size_t smem_final = smem + (size_t) (kFinalThreads / 32) * per_warp_final;
+    const uint32_t fthreads = L >= 4096 ? kFinalThreadsWide : kFinalThreads;
+    const size_t smem_final_p = smem + (size_t) (fthreads / 32) * per_warp_final;
     timing_mark(0, st);
     k_prep<<<1, 1024, (size_t) L * 12, st>>>(p);
     timing_mark(1, st);
@@ -1877,12 +1883,13 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &per_sm, rev ? k_final<true> : k_final<false>, kFinalThreads, smem_final) !=
+                &per_sm, rev ? k_final<true> : k_final<false>, fthreads, smem_final_p) !=
                 cudaSuccess || per_sm < 1)
             per_sm = 1;
-        const unsigned gp = std::min<unsigned>(gf, (unsigned) (per_sm * std::max(sms, 1)));
-        if (rev) k_final<true><<<gp, kFinalThreads, smem_final, st>>>(p);
-        else k_final<false><<<gp, kFinalThreads, smem_final, st>>>(p);
+        const unsigned need = (unsigned) ((nblk + fthreads - 1) / fthreads);
+        const unsigned gp = std::min<unsigned>(need, (unsigned) (per_sm * std::max(sms, 1)));
+        if (rev) k_final<true><<<gp, fthreads, smem_final_p, st>>>(p);
+        else k_final<false><<<gp, fthreads, smem_final_p, st>>>(p);
     }
     timing_mark(5, st);
     if (g_timing.on && g_timing.used < g_timing.cap) ++g_timing.used;
