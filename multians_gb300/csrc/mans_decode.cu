@@ -2056,6 +2056,10 @@ struct BatchLayout {
     size_t n_sync, n_walk, n_scan, n_final, n_items;
     bool any_capture;
     size_t smem_sync, smem_walk, smem_final, smem_prep;
+    // G-pass and final-pass launches per table class (0: L <= 1024, 1:
+    // larger), each with its own shared memory: a batch's large tables
+    // then leave the small-table streams at their own occupancy
+    size_t n_sync_c[2], n_final_c[2], smem_sync_c[2], smem_final_c[2];
     size_t walk_list;     // [n_walk] stream of each merge-walk CTA (device-built)
     uint32_t walk_grid;   // persistent merge-walk grid
 };
@@ -2073,12 +2077,16 @@ static uint32_t stage_cap_for(double per_unit, uint32_t B) {
 
 constexpr uint64_t kBatchRegionMax = 8192;   // units
 
+static int batch_class(uint32_t L) { return L <= 1024 ? 0 : 1; }
+
 static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hint,
                       std::vector<BatchStreamPlan>& plans, BatchLayout& lay) {
     plans.assign(n, BatchStreamPlan{});
     size_t data = 0, flag_words = 0;
     lay.n_sync = lay.n_walk = lay.n_scan = lay.n_final = 0;
     lay.any_capture = false;
+    for (int c = 0; c < 2; ++c)
+        lay.n_sync_c[c] = lay.n_final_c[c] = lay.smem_sync_c[c] = lay.smem_final_c[c] = 0;
     lay.smem_sync = lay.smem_walk = lay.smem_final = lay.smem_prep = 0;
     // A batch finds its parallelism across streams: regions are sized so the
     // whole batch gives about one G-pass wave of lanes (152 SMs x 16 warps),
@@ -2132,20 +2140,25 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
         flag_words += sp.ntiles + 4;
         sp.stage_cap = stage_cap_for((double) d[i].n_out / (double) d[i].n_units,
                                      sp.cfg.block_units);
+        const int cls = batch_class(d[i].L);
         lay.n_sync += (sp.nreg + kSyncThreads - 1) / kSyncThreads;
+        lay.n_sync_c[cls] += (sp.nreg + kSyncThreads - 1) / kSyncThreads;
         lay.n_walk += walk_ctas(sp.nreg);
         lay.smem_walk = std::max(lay.smem_walk, walk_smem(d[i].L, sp.cfg.capture_bytes != 0));
         lay.n_scan += sp.ntiles;
         lay.n_final += (sp.nblk + kFinalThreads - 1) / kFinalThreads;
+        lay.n_final_c[cls] += (sp.nblk + kFinalThreads - 1) / kFinalThreads;
         lay.any_capture |= sp.cfg.capture_bytes != 0;
         const size_t tab = ((size_t) d[i].L * 8 + 15) & ~(size_t) 15;
-        lay.smem_sync = std::max(lay.smem_sync,
-                                 sync_smem(d[i].L, kSyncThreads, sp.cfg.capture_bytes != 0));
+        const size_t ss = sync_smem(d[i].L, kSyncThreads, sp.cfg.capture_bytes != 0);
+        lay.smem_sync = std::max(lay.smem_sync, ss);
+        lay.smem_sync_c[cls] = std::max(lay.smem_sync_c[cls], ss);
         const uint32_t tile_bytes = (sp.cfg.block_units + 4) * 4;
         const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
-        lay.smem_final = std::max(lay.smem_final,
-                                  tab + (size_t) (kFinalThreads / 32) *
-                                            ((size_t) 32 * tile_stride + 16 + sp.stage_cap + 16));
+        const size_t sf = tab + (size_t) (kFinalThreads / 32) *
+                                    ((size_t) 32 * tile_stride + 16 + sp.stage_cap + 16);
+        lay.smem_final = std::max(lay.smem_final, sf);
+        lay.smem_final_c[cls] = std::max(lay.smem_final_c[cls], sf);
         lay.smem_prep = std::max(lay.smem_prep, (size_t) d[i].L * 12);
     }
     lay.n_items = lay.n_sync + lay.n_scan + lay.n_final;   // merge walks: built on the device
@@ -2297,6 +2310,8 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
     for (uint32_t i = 0; i < n; ++i)
         if (b->plans[i].active) order.push_back(i);
     std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        const int cx = batch_class(streams[x].L), cy = batch_class(streams[y].L);
+        if (cx != cy) return cx < cy;   // one launch per table class
         return (double) streams[x].n_out / (double) b->plans[x].nreg >
                (double) streams[y].n_out / (double) b->plans[y].nreg;   // symbols per region
     });
@@ -2304,6 +2319,8 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         for (size_t r = 0; r < b->plans[i].nreg; r += kSyncThreads)
             b->items[is++] = {i, (uint32_t) r, 0, 0};
     std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+        const int cx = batch_class(streams[x].L), cy = batch_class(streams[y].L);
+        if (cx != cy) return cx < cy;
         return streams[x].n_out > streams[y].n_out;
     });
     for (const uint32_t i : order) {
@@ -2374,8 +2391,10 @@ int mans_batch_decode(mans_batch* b, void* stream) {
     timing_mark(0, st);
     k_prep_batch<<<b->n, 1024, L.smem_prep, st>>>(ps);
     timing_mark(1, st);
-    if (L.n_sync)
-        k_gwalk_batch<<<(unsigned) L.n_sync, kSyncThreads, L.smem_sync, st>>>(ps, items);
+    for (int c = 0, at = 0; c < 2; at += (int) L.n_sync_c[c], ++c)
+        if (L.n_sync_c[c])
+            k_gwalk_batch<<<(unsigned) L.n_sync_c[c], kSyncThreads, L.smem_sync_c[c], st>>>(
+                ps, items + at);
     timing_mark(2, st);
     if (L.n_walk) {
         // ticket words: 0 scan tiles, 1 merge-walk items, 2 next item
@@ -2392,13 +2411,15 @@ int mans_batch_decode(mans_batch* b, void* stream) {
     if (L.n_final && L.any_capture)
         k_copy_batch<<<(unsigned) L.n_final, kCopyThreads, 0, st>>>(
             ps, items + L.n_sync + L.n_scan);
-    if (L.n_final)
-        k_final_batch<<<(unsigned) L.n_final, kFinalThreads, L.smem_final, st>>>(
-            ps, items + L.n_sync + L.n_scan);
+    for (int c = 0, at = 0; c < 2; at += (int) L.n_final_c[c], ++c)
+        if (L.n_final_c[c])
+            k_final_batch<<<(unsigned) L.n_final_c[c], kFinalThreads, L.smem_final_c[c], st>>>(
+                ps, items + L.n_sync + L.n_scan + at);
     timing_mark(5, st);
     if (g_timing.on && g_timing.used < g_timing.cap) ++g_timing.used;
-    g_last_launches = 1 + (L.n_sync ? 1 : 0) + (L.n_walk ? 2 : 0) + (L.n_scan ? 1 : 0) +
-                      (L.n_final ? (L.any_capture ? 2 : 1) : 0);
+    g_last_launches = 1 + (L.n_sync_c[0] ? 1 : 0) + (L.n_sync_c[1] ? 1 : 0) +
+                      (L.n_walk ? 2 : 0) + (L.n_scan ? 1 : 0) + (L.n_final_c[0] ? 1 : 0) +
+                      (L.n_final_c[1] ? 1 : 0) + (L.n_final && L.any_capture ? 1 : 0);
     return cudaGetLastError() == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
 }
 
