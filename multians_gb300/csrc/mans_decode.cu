@@ -1,6 +1,8 @@
 // Plain single-stream decode: the reference's four phases (guessed-state
 // decode, sync extension, exclusive prefix sum, final write pass) rebuilt
-// as three sm_103a kernels that never stop for the host.
+// as sm_103a kernels that never stop for the host (k_prep, k_gwalk,
+// k_wwalk, k_scan, then k_final, or with symbol capture k_copy and
+// k_final_fb), and the batched form of the same kernels.
 //
 // Geometry.  The stream is cut into blocks of B units (final-pass work
 // items) and regions of nb blocks (sync work items, R = nb * B units).
@@ -33,6 +35,12 @@
 //           (bit, state) and output offset D_k + count.  The block is
 //           decoded and its symbols written (the reference's phase 4,
 //           src/multians_gpu_decoder.cu:492-573).
+//  capture  (long streams, 2+ bits per symbol) k_gwalk and k_wwalk also
+//           keep the symbols they decode, count c of Gamma_k at byte c of
+//           region k's slice; k_copy then copies every block whose owner's
+//           symbols are in a slice (Gamma_r's, or the owner's own) and lists
+//           the warps that hold any other block for k_final_fb, the k_final
+//           decode over those warps only.
 //
 // No pass waits on another thread: correctness needs only that every walk
 // ends inside its slots, which the host checks and cures by re-planning.
