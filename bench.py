@@ -9,7 +9,7 @@ seeded synthetic uint8 symbols, the reference's table generator and encoder
 (the library's C++ implementation of them), one raw stream.
 
   value   decoded GB/s (decoded bytes / s) with the stream and the output
-          resident in HBM; each step is one full decode (four kernels).
+          resident in HBM; each step is one full decode (five or six kernels).
   e2e     the same metric through the public C ABI with host buffers: per
           step the pinned-host units and table go host->device, the decode
           runs, the decoded bytes come back device->host; steps pipelined

@@ -199,7 +199,8 @@ static_assert(sizeof(WJob) == 32, "job record layout");
 // below unit 16(w+1) + 36 < 16(w+4), the start of the new chunk: a chunk
 // copied in round r is first read in round r + 2, and round r waits only
 // for the copies of round r - 2.  The small ring (272 bytes a lane) keeps
-// 20 warps of walks resident per SM.
+// 20 warps of walks resident per SM (16 with symbol capture, whose rings
+// take shared memory too).
 constexpr uint32_t kChunk = 16;                    // units per ring slot
 constexpr uint32_t kRingSlots = 4;
 constexpr uint32_t kRingUnits = kChunk * kRingSlots;
