@@ -124,3 +124,32 @@ def test_table_upload_rejects_bad_tables(mg, oracle_lib):
     assert mg.lib().mans_table_upload(p, 1, ctypes.byref(out)) == mg.Status.ERR_ARG
     assert mg.lib().mans_table_upload(None, 1024, ctypes.byref(out)) == mg.Status.ERR_ARG
     assert mg.lib().mans_aux_free(None) == 0 and mg.lib().mans_table_free(None) == 0
+
+
+@pytest.mark.parametrize("L", [1024, 2048, 4096, 8192])
+def test_plan_invariants(mg, L):
+    """The planner's geometry over sizes and entropies: block sizes from the
+    supported set, odd region lengths, walk slots within bounds, capture
+    slices 16-byte multiples holding a region's expected symbols, and (for
+    streams long enough to fill it) at most one wave of G-pass lanes."""
+    # resident lanes of the capturing G pass (shared memory bounds them)
+    lanes_capture = {1024: 152 * 2 * 256, 2048: 152 * 3 * 128, 4096: 152 * 2 * 128}
+    for n_out in (10_000, 3_000_000, 64 << 20, 256 << 20, 2 << 30):
+        for bps in (0.67, 1.5, 3.8, 6.0, 8.6):
+            n_units = max(1, int(n_out * bps / 32))
+            p = mg.plan(n_units, n_out, L)
+            assert p["block_units"] in (4, 8, 16)
+            assert p["region_blocks"] % 2 == 1 and p["region_blocks"] >= 8
+            assert 1 <= p["walk_slots"] <= 12
+            cap = p["capture_bytes"]
+            assert cap % 16 == 0
+            want_cap = n_units >= 16 << 20 and bps >= 2.0 and L <= 4096
+            assert (cap > 0) == want_cap, (n_out, bps, L, p)
+            R = p["block_units"] * p["region_blocks"]
+            if cap:
+                assert cap >= n_out / n_units * R   # a region's symbols fit
+                nblk = n_units // p["block_units"] + 1
+                nreg = -(-nblk // p["region_blocks"])
+                if R < 4096:   # not clamped by the longest region
+                    assert nreg <= lanes_capture[L], (nreg, p)
+            assert mg.aux_size(n_units, p) > 0
