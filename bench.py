@@ -365,6 +365,11 @@ def run_ours(args, ws, rank, local):
     e2e_ok = e2e_ok and bool(np.array_equal(out_h2[last].numpy(), st.symbols[::-1]))
     e2e_ok = e2e_ok and aux_status(aux, stream) == 0
     del units2, table2, out2, out_h2
+    if ws > 1:
+        # the slowest rank's step times, as for the device-resident value
+        t = torch.tensor([e2e_ms, e2e_serial_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms, e2e_serial_ms = float(t[0].item()), float(t[1].item())
 
     if rank != 0:
         if ws > 1:
