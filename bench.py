@@ -143,6 +143,25 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(values, device=None):
+    """Each value's maximum over the ranks (one all_reduce; the identity in
+    a single process): the slowest replica sets a multi-GPU run's times."""
+    import torch
+    import torch.distributed as dist
+    vals = [float(v) for v in values]
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return vals
+    t = torch.tensor(vals, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def replica_rate(per_rank, ws, ms):
+    """Whole-job GB/s of ws replicas that each process per_rank bytes, over
+    the slowest replica's ms."""
+    return ws * per_rank / (ms / 1e3) / 1e9
+
+
 def make_workload(args, rank):
     from multians_gb300 import host
     n = int(args.mb * (1 << 20))
@@ -285,10 +304,7 @@ def run_ours(args, ws, rank, local):
     status |= aux_status(aux, stream)
     bit_exact = bit_exact and bool(torch.equal(out, torch.from_numpy(
         np.ascontiguousarray(st.symbols[::-1])).to(dev))) and status == 0
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    (total_ms,) = max_over_ranks([total_ms], dev)
 
     # e2e: host buffers through the C ABI, copies inside the timed region.
     # Serial: per step H2D, decode, D2H on one stream.  Pipelined, the way a
@@ -365,11 +381,8 @@ def run_ours(args, ws, rank, local):
     e2e_ok = e2e_ok and bool(np.array_equal(out_h2[last].numpy(), st.symbols[::-1]))
     e2e_ok = e2e_ok and aux_status(aux, stream) == 0
     del units2, table2, out2, out_h2
-    if ws > 1:
-        # the slowest rank's step times, as for the device-resident value
-        t = torch.tensor([e2e_ms, e2e_serial_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms, e2e_serial_ms = float(t[0].item()), float(t[1].item())
+    # the slowest rank's step times, as for the device-resident value
+    e2e_ms, e2e_serial_ms = max_over_ranks([e2e_ms, e2e_serial_ms], dev)
 
     if rank != 0:
         if ws > 1:
@@ -377,7 +390,7 @@ def run_ours(args, ws, rank, local):
         return
 
     ms = total_ms / args.steps
-    value = ws * n / (ms / 1e3) / 1e9
+    value = replica_rate(n, ws, ms)
     hbm, peak_kind = measured_peaks()
     comp_bytes = st.n_units * 4
     # dominant kernel and its algorithmic bytes per launch
@@ -428,10 +441,10 @@ def run_ours(args, ws, rank, local):
                      "frac": round(achieved / hbm, 4), "traffic": traffic,
                      "alg_bytes_per_launch": alg},
         "cpu_baseline": cpu,
-        "e2e": {"value": round(ws * n / (e2e_ms / 1e3) / 1e9, 3), "unit": "GB/s",
+        "e2e": {"value": round(replica_rate(n, ws, e2e_ms), 3), "unit": "GB/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "bit_exact": e2e_ok,
                 "pipelined": "2 buffer sets; H2D, decode, D2H on 3 streams",
-                "serial_value": round(ws * n / (e2e_serial_ms / 1e3) / 1e9, 3)},
+                "serial_value": round(replica_rate(n, ws, e2e_serial_ms), 3)},
         "gpu_launches": launches_per * args.steps,
         "clocks": clk.summary(),
         "gen_seconds": round(gen_s, 2),

@@ -214,11 +214,12 @@ def run_batched(args, ws, rank, local):
         b2.close()
         del d_units2, d_out2, h_out2
     b.close()
+    from bench import max_over_ranks, measured_peaks, replica_rate
+    batch_ms, e2e_ms, e2e_serial_ms = max_over_ranks([batch_ms, e2e_ms, e2e_serial_ms], dev)
     if rank != 0:
         return
-    from bench import measured_peaks
     hbm, kind = measured_peaks()
-    value = ws * total_sym / (batch_ms / 1e3) / 1e9
+    value = replica_rate(total_sym, ws, batch_ms)
     alg = (total_comp + total_sym) / (batch_ms / 1e3) / 1e9
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": ws,
@@ -305,9 +306,10 @@ def run_encode(args, ws, rank, local):
     host_s = time.perf_counter() - t0
     exact = (n_units, fb, fs) == (ref.n_units, ref.first_bit, ref.first_state) and bool(
         np.array_equal(units.cpu().numpy().view(np.uint32), ref.units))
+    from bench import max_over_ranks
+    ms, e2e_med = max_over_ranks([statistics.median(t_dev), statistics.median(t_e2e)], dev)
     if rank != 0:
         return
-    ms = statistics.median(t_dev)
     line = {
         "metric": "encoded GB/s on 1 GB300 (source bytes / s), bit-exact with the reference encoder",
         "value": round(ws * n / (ms / 1e3) / 1e9, 3), "unit": "GB/s", "n_gpus": ws,
@@ -318,7 +320,7 @@ def run_encode(args, ws, rank, local):
                    "n_symbols": n, "n_units": n_units, "seed": args.seed,
                    "step": "histogram + host table build + 6 encode kernels"},
         "bit_exact": exact,
-        "e2e": {"value": round(ws * n / (statistics.median(t_e2e) / 1e3) / 1e9, 3),
+        "e2e": {"value": round(ws * n / (e2e_med / 1e3) / 1e9, 3),
                 "unit": "GB/s", "h2d_bytes_per_step": n, "d2h_bytes_per_step": int(u2.numel()) * 4},
         "cpu_baseline": {"value": round(n / host_s / 1e9, 4), "unit": "GB/s", "cores": 1,
                          "kind": "port", "sample": "the whole stream, the library's host encoder "
@@ -330,11 +332,24 @@ def run_encode(args, ws, rank, local):
 
 
 def run(args, ws, rank, local):
-    if args.workload == "encode":
-        return run_encode(args, ws, rank, local)
-    if args.workload == "batched":
-        return run_batched(args, ws, rank, local)
-    if args.workload == "served":
-        from multians_gb300 import serve_bench
-        return serve_bench.run(args, ws, rank, local)
-    raise ValueError(args.workload)
+    """Under torchrun every rank runs its own replica of the workload; the
+    reported times are the slowest rank's (bench.max_over_ranks)."""
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        dev = torch.device("cuda", local)
+        torch.cuda.set_device(dev)
+        dist.init_process_group("nccl", device_id=dev)
+    try:
+        if args.workload == "encode":
+            return run_encode(args, ws, rank, local)
+        if args.workload == "batched":
+            return run_batched(args, ws, rank, local)
+        if args.workload == "served":
+            from multians_gb300 import serve_bench
+            return serve_bench.run(args, ws, rank, local)
+        raise ValueError(args.workload)
+    finally:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
