@@ -174,3 +174,36 @@ def test_default_capture_large_stream(mg):
                  st.first_bit, aux, {})
     assert aux_status(aux) == 0
     assert np.array_equal(out.cpu().numpy()[::-1], st.symbols)
+
+
+def test_capture_single_symbol_and_bad_table(mg, oracle_lib):
+    """With capture asked for, a single-symbol table still fills the output
+    (the copy pass does it) and a bad table is still rejected."""
+    import torch
+    O = oracle_lib
+    sym = np.full(50_000, 17, dtype=np.uint8)
+    st = O.encode(sym, 1024)
+    assert mg.table_check(st.table) == 1
+    got, p = _decode(mg, st, {"capture_bytes": 1024})
+    assert p["capture_bytes"] == 1024 and np.array_equal(got, sym)
+    st = O.make_stream(seed=7900, lam=0.05, n=100_000, L=1024)
+    bad = st.table.copy()
+    bad[5] = (bad[5] & 0x00ffffff) | (15 << 24)
+    out = torch.empty(st.n, dtype=torch.uint8, device="cuda")
+    with pytest.raises(mg.MansError):
+        mg.decode(_dev(st.units), st.n_units, st.n, _dev(bad), st.first_state, st.first_bit,
+                  L=st.L, out=out, cfg={"capture_bytes": 4096})
+
+
+@pytest.mark.parametrize("lam", [0.05, 0.5])
+def test_capture_forced_at_8192_states(mg, oracle_lib, lam):
+    """The largest table (64 KB in shared memory) with capture forced on:
+    the capturing G pass, walks and fallback still fit and agree."""
+    O = oracle_lib
+    st = O.make_stream(seed=7950 + int(lam * 10), lam=lam, n=250_000, L=8192)
+    want = O.decode_seq(st)
+    got, p = _decode(mg, st, {"capture_bytes": 8192})
+    assert p["capture_bytes"] == 8192
+    assert np.array_equal(got, want)
+    rev, _ = _decode(mg, st, {"capture_bytes": 8192}, source_order=True)
+    assert np.array_equal(rev, st.symbols)
