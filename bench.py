@@ -413,6 +413,17 @@ def run_ours(args, ws, rank, local):
                 parts = ln.strip().split("\t")
                 if len(parts) == 3 and parts[0] == dom and parts[1] == wl:
                     traffic = int(parts[2])
+    # instruction-issue utilisation of the kernels (ncu, issue active per
+    # scheduler, from the committed profile of this workload): the decode is
+    # bound by issue, not by HBM
+    issue = {}
+    isf = os.path.join(ROOT, "profiles", "issue_per_kernel.txt")
+    if os.path.exists(isf):
+        with open(isf) as f:
+            for ln in f:
+                parts = ln.strip().split("\t")
+                if len(parts) == 3 and parts[1] == wl:
+                    issue[parts[0]] = float(parts[2])
     per_sorted = sorted(per_ms)
     cpu = None
     if not args.no_cpu_baseline:
@@ -440,6 +451,8 @@ def run_ours(args, ws, rank, local):
                      "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": traffic,
                      "alg_bytes_per_launch": alg},
+        "issue_roofline": {"issue_active_pct": issue, "dominant": dom,
+                           "source": "ncu smsp__issue_active (profiles/)"} if issue else None,
         "cpu_baseline": cpu,
         "e2e": {"value": round(replica_rate(n, ws, e2e_ms), 3), "unit": "GB/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "bit_exact": e2e_ok,
