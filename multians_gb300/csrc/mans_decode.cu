@@ -346,7 +346,7 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
     // the pass is bound by instruction issue: a unit load every step beats
     // a refill branch that some lane of the warp takes on most steps
     // (measured: capturing 0.430 -> 0.398 ms, uncaptured 0.345 -> 0.310 ms)
-    SCursorT<false> A;
+    SCursor A;
     uint32_t ca = 0;
     // the capture rows start on a 4 KB boundary, so a row address is the
     // lane's column OR the row offset (one logic operation per step)
@@ -1028,7 +1028,7 @@ __device__ __forceinline__ bool final_warp(const DecodeParams& p, uint32_t tb, u
     if (dec) {
         const uint32_t pos_cap = p.B * 32 + kMaxBits + 1;
         const uint32_t full = off_nx >= off ? (uint32_t) min(off_nx - off, 0xffffffffull) : 0u;
-        SCursorLazy c;
+        SCursor c;
         const UnitSrc ts{tile, u0, ~0u, tile_units - 1};
         const uint64_t bs = (uint64_t) b * p.B * 32;   // cursor units are global indices
         c.init(ts, bs, bs + (rec.x & 0xffu), tb + 8u * min(rec.x >> 8, p.L - 1));

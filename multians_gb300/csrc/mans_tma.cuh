@@ -98,27 +98,19 @@ struct UnitSrc {
 // and when o reaches 32 shifts the window by one unit (selects, no
 // branch).
 //
-// Where the unit a refill takes comes from is a trade between latency and
-// shared-memory bandwidth:
-//  * kLazy = false: every step loads it, next to the table entry and before
-//    either is needed.  A load issued only on the refilling lanes would make
-//    the whole warp wait for it at the next refill of any lane (one
-//    register, one scoreboard) unless enough other warps hide that wait.
-//    Used where few warps run (the merge-walk passes).
-//  * kLazy = true: it is already in a register (nu); a refill consumes it
-//    and loads the following unit.  A step takes at most kMaxBits bits, so
-//    refills are at least two steps apart and only refilling lanes touch
-//    shared memory for units: about a fifth of the unit wavefronts.  Used
-//    where many warps share an SM and wavefronts bound the kernel.
-template <bool kLazy>
-struct SCursorT {
+// Every step loads the unit a refill would take, next to the table entry
+// and before either is needed.  Loading it only on refilling lanes (a
+// branch some lane of the warp takes on most steps, about a fifth of the
+// unit wavefronts) was measured slower in every pass on GB300: the passes
+// are bound by instruction issue or by the walk chain, not by shared-memory
+// wavefronts (G pass 0.345 -> 0.310 ms, final pass 0.349 -> 0.339 ms).
+struct SCursor {
     uint2 e;         // table entry of the current state
     uint32_t a;      // shared address of that entry
     uint32_t w0, w1; // window: units next - 2 and next - 1
     uint32_t o;      // bit offset of the next codeword in w0:w1 (< 32)
     uint32_t pos;    // bit position of the next codeword (relative)
     uint32_t next;   // global index of the next unit a refill takes
-    uint32_t nu;     // that unit (kLazy only)
 
     __device__ __forceinline__ void init(const UnitSrc& src, uint64_t origin, uint64_t abs,
                                          uint32_t entry_addr) {
@@ -130,12 +122,11 @@ struct SCursorT {
         w0 = src(u);
         w1 = src(u + 1);
         next = u + 2;
-        if (kLazy) nu = src(next);
     }
 
     // One step; returns y (mask | k << 16 | count-or-symbol << 24).
     __device__ __forceinline__ uint32_t step(const UnitSrc& src) {
-        const uint32_t u = kLazy ? nu : src(next);
+        const uint32_t u = src(next);
         const uint32_t y = e.y;
         const uint32_t bits = __funnelshift_r(w0, w1, o);
         a = e.x + ((bits & y & 0xffffu) << 3);
@@ -148,12 +139,9 @@ struct SCursorT {
         w1 = r ? u : w1;
         o = r ? o - 32 : o;
         next += r ? 1u : 0u;
-        if (kLazy && r) nu = src(next);
         return y;
     }
 };
 
-using SCursor = SCursorT<false>;
-using SCursorLazy = SCursorT<true>;
 
 }  // namespace mans
