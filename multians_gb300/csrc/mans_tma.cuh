@@ -143,5 +143,4 @@ struct SCursor {
     }
 };
 
-
 }  // namespace mans

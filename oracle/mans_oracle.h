@@ -2,8 +2,8 @@
  * CPU oracle for the MULTIANS tANS decode path -- TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of the reference's host algorithms (table generator,
- * encoder, multicore decoder) used as the checker of the CUDA decoder and as
- * the timed CPU baseline.  Only tests/, __graft_entry__.smoke() and bench.py's
+ * encoder, multicore decoder) that the CUDA decoder's output is compared
+ * against, and the timed CPU baseline.  Only tests/, __graft_entry__.smoke() and bench.py's
  * CPU-baseline leg load it.  The product (multians_gb300/) never does.
  *
  * Each function cites the reference file:line it follows (paths relative to
