@@ -248,7 +248,9 @@ typedef struct {
 #define MANS_REQ_SOURCE_ORDER 0x2u  /* output in source order (MANS_DECODE_SOURCE_ORDER) */
 #define MANS_REQ_CONTAINER 0x4u     /* units points at a host container of n_units
                                        bytes; table, n_out, first_state / first_bit
-                                       come from it (out must hold n_symbols) */
+                                       come from it (out must hold n_symbols); its
+                                       table is added as by mans_server_add_table
+                                       (identical tables shared, kept until destroy) */
 #define MANS_REQ_NO_CAPTURE 0x8u    /* decode without symbol capture (MANS_DECODE_NO_CAPTURE) */
 
 typedef struct {
@@ -292,8 +294,9 @@ int mans_server_poll(mans_server* s, mans_completion* out, size_t cap, size_t* n
 int mans_server_stats_get(mans_server* s, mans_server_stats* out);
 /* The clock of arrival_ns / done_ns (CLOCK_MONOTONIC, nanoseconds). */
 uint64_t mans_server_now_ns(void);
-/* Finishes the batches in flight, drops requests not yet launched, joins
- * the worker and frees everything. */
+/* Finishes the batches in flight, drops requests not yet launched (no
+ * completion; their input copies end before it returns), joins the worker
+ * and frees everything. */
 int mans_server_destroy(mans_server* s);
 
 /* Host-side data preparation (the reference's ANSTableGenerator +

@@ -49,12 +49,14 @@ def pack(units, n_units: int, n_symbols: int, table, first_state: int, first_bit
     """A container (uint8 array, or written into `out`, e.g. pinned memory)."""
     u = np.ascontiguousarray(units, dtype=np.uint32)
     t = np.ascontiguousarray(table, dtype=np.uint32)
+    if not 0 <= n_units <= u.size:
+        raise ValueError(f"n_units {n_units} outside the {u.size} units given")
     lb = _sig()
     size = int(lb.mans_container_size(n_units, t.size))
     buf = np.empty(size, dtype=np.uint8) if out is None else out
     written = ctypes.c_size_t(0)
-    ptr = buf.ctypes.data if isinstance(buf, np.ndarray) else buf.data_ptr()
-    check(lb.mans_container_write(ptr, size, u.ctypes.data_as(_u32p), n_units, n_symbols,
+    ptr, cap = _span(buf)
+    check(lb.mans_container_write(ptr, cap, u.ctypes.data_as(_u32p), n_units, n_symbols,
                                   t.ctypes.data_as(_u32p), t.size, first_state, first_bit,
                                   ctypes.byref(written)), "mans_container_write")
     return buf
@@ -65,9 +67,19 @@ def pack_encoded(st, out=None) -> np.ndarray:
     return pack(st.units, st.n_units, st.n, st.table, st.first_state, st.first_bit, out=out)
 
 
+def _span(buf) -> tuple[int, int]:
+    """Address and size in bytes of a contiguous numpy array or host tensor."""
+    if isinstance(buf, np.ndarray):
+        if not buf.flags.c_contiguous:
+            raise ValueError("container buffer must be contiguous")
+        return buf.ctypes.data, buf.nbytes
+    if not buf.is_contiguous() or buf.is_cuda:
+        raise ValueError("container buffer must be a contiguous host tensor")
+    return buf.data_ptr(), buf.numel() * buf.element_size()
+
+
 def parse(buf) -> Info:
-    ptr = buf.ctypes.data if isinstance(buf, np.ndarray) else buf.data_ptr()
-    size = buf.nbytes if isinstance(buf, np.ndarray) else buf.numel() * buf.element_size()
+    ptr, size = _span(buf)
     info = InfoC()
     check(_sig().mans_container_parse(ptr, size, ctypes.byref(info)), "mans_container_parse")
     return Info(int(info.n_symbols), int(info.n_units), int(info.L), int(info.first_state),

@@ -65,8 +65,9 @@ size_t mans_container_size(uint64_t n_units, uint32_t L) {
 int mans_container_write(void* buf, size_t cap, const uint32_t* units, uint64_t n_units,
                          uint64_t n_symbols, const uint32_t* table, uint32_t L,
                          uint32_t first_state, uint32_t first_bit, size_t* size) {
+    // the same limits parse enforces (n_units also keeps the size from wrapping)
     if (!buf || !units || !table || L < 2 || L > 8192 || first_state < L ||
-        first_state >= 2 * L || first_bit > 32)
+        first_state >= 2 * L || first_bit > 32 || n_units > 0xffffffffull)
         return MANS_ERR_ARG;
     const size_t need = mans_container_size(n_units, L);
     if (cap < need) return MANS_ERR_AUX_SMALL;

@@ -497,6 +497,9 @@ struct mans_server {
             if (!fired) cv.wait_for(lk, std::chrono::milliseconds(2));
         }
         lk.unlock();
+        // requests admitted but not launched may still have input copies in
+        // flight from the caller's memory: let them end before returning
+        cudaStreamSynchronize(copy_stream);
         for (Req* q : pending) delete q;
         for (Req* q : ready) delete q;
         pending.clear();
