@@ -1695,8 +1695,8 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
     // when three meeting distances are longer): measured over 0.67 .. 8.6
     // bits per symbol and L = 1024 / 4096, between about 2.5 and 4 meeting
     // distances is best.  With capture the lanes are those the capturing G
-    // pass keeps resident (16 warps per SM at L = 1024, 8 at L = 2048 and
-    // 4096: the rings and the table fill shared memory), and R may grow to
+    // pass keeps resident (16 warps per SM at L = 1024, 12 at L = 2048, 8 at
+    // L = 4096: the rings and the table fill shared memory), and R may grow to
     // 4096 units to keep them one wave.
     const uint64_t tail = std::max<uint64_t>(256, 4ull * L);
     const double meet = mean_meeting_units(L, bps);
