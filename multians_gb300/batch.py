@@ -41,16 +41,26 @@ def _sig():
     return L
 
 
+def _addr(t, nbytes: int, what: str):
+    """Device address of a CUDA tensor of at least `nbytes` bytes (None
+    passes through: descriptors used only for sizing carry no buffers)."""
+    if t is None:
+        return None
+    from .decoder import _dev_ptr
+    return _dev_ptr(t, nbytes, what).value
+
+
 def desc(units, n_units, out, n_out, table, L, first_state, first_bit,
          source_order: bool = False, capture: bool = True) -> StreamDesc:
     """A stream descriptor from CUDA tensors (units/table int32 or uint32
     views); ``source_order`` writes the output in source order, ``capture``
-    False keeps the stream out of symbol capture."""
+    False keeps the stream out of symbol capture.  Tensors shorter than the
+    sizes given are refused (the batch kernels see only addresses)."""
     from ._lib import DECODE_NO_CAPTURE, DECODE_SOURCE_ORDER
     flags = (DECODE_SOURCE_ORDER if source_order else 0) | (0 if capture else DECODE_NO_CAPTURE)
-    return StreamDesc(units.data_ptr() if units is not None else None, int(n_units),
-                      out.data_ptr() if out is not None else None, int(n_out),
-                      table.data_ptr() if table is not None else None, int(L),
+    return StreamDesc(_addr(units, 4 * int(n_units), "units"), int(n_units),
+                      _addr(out, int(n_out), "out"), int(n_out),
+                      _addr(table, 4 * int(L), "table"), int(L),
                       int(first_state), int(first_bit), flags)
 
 

@@ -26,11 +26,22 @@ def _stream_ptr(stream):
     return ctypes.c_void_p(stream.cuda_stream)
 
 
-def _dev_ptr(t):
+def _dev_ptr(t, nbytes: int = 0, what: str = "tensor"):
+    """Device address of a contiguous CUDA tensor holding at least `nbytes`
+    bytes on the current device.  The C calls see only addresses, so a
+    short buffer has to be refused here, before any kernel reads or writes
+    past its end."""
     if not t.is_cuda:
-        raise ValueError("expected a CUDA tensor")
+        raise ValueError(f"{what}: expected a CUDA tensor")
     if not t.is_contiguous():
-        raise ValueError("expected a contiguous tensor")
+        raise ValueError(f"{what}: expected a contiguous tensor")
+    have = t.numel() * t.element_size()
+    if have < nbytes:
+        raise ValueError(f"{what}: {have} bytes, the call needs {nbytes}")
+    if t.device.index is not None:
+        cur = _torch().cuda.current_device()
+        if t.device.index != cur:
+            raise ValueError(f"{what}: on {t.device}, the current device is cuda:{cur}")
     return ctypes.c_void_p(t.data_ptr())
 
 
@@ -92,8 +103,10 @@ class CUHDGPUDecoder:
                                                    int(number_of_states), {})))
         st = ctypes.c_uint32(0)
         rc = lib().mans_decode_sync(
-            _dev_ptr(input), int(input_size), _dev_ptr(output), int(output_size),
-            _dev_ptr(table), int(number_of_states), int(initial_state), int(initial_bit),
+            _dev_ptr(input, 4 * int(input_size), "input"), int(input_size),
+            _dev_ptr(output, int(output_size), "output"), int(output_size),
+            _dev_ptr(table, 4 * int(number_of_states), "table"), int(number_of_states),
+            int(initial_state), int(initial_bit),
             _dev_ptr(aux.get()), aux.get().numel(), None, _stream_ptr(stream), ctypes.byref(st))
         check(rc, "CUHDGPUDecoder.decode")
         return int(st.value)
@@ -103,8 +116,10 @@ def decode_async(units, n_units: int, out, n_out: int, table, L: int, first_stat
                  first_bit: int, aux, cfg: dict | None = None, stream=None) -> None:
     """Enqueues one decode (mans_decode); no host synchronisation."""
     c = Cfg(**(cfg or {}))
-    rc = lib().mans_decode(_dev_ptr(units), int(n_units), _dev_ptr(out), int(n_out),
-                           _dev_ptr(table), int(L), int(first_state), int(first_bit),
+    rc = lib().mans_decode(_dev_ptr(units, 4 * int(n_units), "units"), int(n_units),
+                           _dev_ptr(out, int(n_out), "out"), int(n_out),
+                           _dev_ptr(table, 4 * int(L), "table"), int(L),
+                           int(first_state), int(first_bit),
                            _dev_ptr(aux), aux.numel(), ctypes.byref(c), _stream_ptr(stream))
     check(rc, "mans_decode")
 
@@ -146,8 +161,10 @@ def decode(units, n_units: int, n_out: int, table, first_state: int, first_bit: 
                    aux_size(n_units, plan(n_units, n_out, L, cfg or {})))
         aux = torch.empty(need, dtype=torch.uint8, device=dev)
     st = ctypes.c_uint32(0)
-    rc = lib().mans_decode_sync(_dev_ptr(units), int(n_units), _dev_ptr(out), int(n_out),
-                                _dev_ptr(table), L, int(first_state), int(first_bit),
+    rc = lib().mans_decode_sync(_dev_ptr(units, 4 * int(n_units), "units"), int(n_units),
+                                _dev_ptr(out, int(n_out), "out"), int(n_out),
+                                _dev_ptr(table, 4 * L, "table"), L,
+                                int(first_state), int(first_bit),
                                 _dev_ptr(aux), aux.numel(),
                                 ctypes.byref(Cfg(**cfg)) if cfg else None,
                                 _stream_ptr(stream), ctypes.byref(st))

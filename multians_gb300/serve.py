@@ -87,11 +87,28 @@ def now_ns() -> int:
     return int(_sig().mans_server_now_ns())
 
 
+def _buf_addr(t, nbytes: int, device_io: bool, what: str) -> int:
+    """Address of a request buffer: a raw address is taken as is; a tensor
+    must be contiguous, on the side `device_io` names and at least `nbytes`
+    long (the worker copies and decodes by address)."""
+    if isinstance(t, int):
+        return t
+    if t.is_cuda != device_io:
+        raise ValueError(f"{what}: a {'CUDA' if device_io else 'host'} tensor is needed "
+                         f"with device_io={device_io}")
+    if not t.is_contiguous():
+        raise ValueError(f"{what}: expected a contiguous tensor")
+    have = t.numel() * t.element_size()
+    if have < nbytes:
+        raise ValueError(f"{what}: {have} bytes, the request needs {nbytes}")
+    return t.data_ptr()
+
+
 def request(units, n_units, out, n_out, table, first_state, first_bit, tag=0,
             arrival_ns=0, device_io=False, source_order=False, capture=True) -> RequestC:
     """A request from tensors (or raw addresses)."""
-    up = units if isinstance(units, int) else units.data_ptr()
-    op = out if isinstance(out, int) else out.data_ptr()
+    up = _buf_addr(units, 4 * int(n_units), device_io, "units")
+    op = _buf_addr(out, int(n_out), device_io, "out")
     flags = ((REQ_DEVICE_IO if device_io else 0) | (REQ_SOURCE_ORDER if source_order else 0) |
              (0 if capture else REQ_NO_CAPTURE))
     return RequestC(up, int(n_units), op, int(n_out), int(table), int(first_state),
@@ -101,10 +118,10 @@ def request(units, n_units, out, n_out, table, first_state, first_bit, tag=0,
 def request_container(container, out, tag=0, arrival_ns=0, source_order=False) -> RequestC:
     """A request whose stream, table and parameters come from a host
     container (multians_gb300.container); `out` holds at least its symbols."""
-    cp = container if isinstance(container, int) else container.data_ptr()
     nbytes = container.numel() * container.element_size()
-    op = out if isinstance(out, int) else out.data_ptr()
-    n_out = out.numel() if hasattr(out, "numel") else 0
+    cp = _buf_addr(container, nbytes, False, "container")
+    n_out = out.numel() * out.element_size()
+    op = _buf_addr(out, n_out, False, "out")
     flags = REQ_CONTAINER | (REQ_SOURCE_ORDER if source_order else 0)
     return RequestC(cp, int(nbytes), op, int(n_out), 0, 0, 0, flags, int(tag), int(arrival_ns))
 
