@@ -280,6 +280,16 @@ def run_ours(args, ws, rank, local):
     status = aux_status(aux, stream)
     bit_exact = bool(torch.equal(out, want)) and status == 0
     del want
+    # what the synchronisation cost beside the algorithmic bytes (read back
+    # from the workspace of the last decode; outside every timed region)
+    try:
+        sync = _lib.sync_stats(aux.data_ptr(), aux.numel(), st.n_units, n, st.L, cfg,
+                               stream.cuda_stream)
+        sync["reread_bytes"] = 4 * sync["walk_units"]
+        sync["reread_frac_of_stream"] = round(sync["walk_units"] / st.n_units, 4)
+        sync["host_round_trips"] = 0
+    except Exception as e:   # a report field: never fails the bench line
+        sync = {"error": str(e)}
 
     # timed region: device-resident decode
     launches_per = mg.lib().mans_last_launch_count()
@@ -447,6 +457,7 @@ def run_ours(args, ws, rank, local):
                             "frac_of_measured": round((comp_bytes + n) / (ms / 1e3) / 1e9 / hbm, 4),
                             "frac_of_8tbs": round((comp_bytes + n) / (ms / 1e3) / 1e9 / 8000, 4)},
         "kernel_ms": {k: round(v, 4) for k, v in mean_k.items()},
+        "sync": sync,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2),
                      "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": traffic,

@@ -117,6 +117,34 @@ int mans_decode(const uint32_t* d_units, size_t n_units,
  * that used d_aux (0 = clean). */
 int mans_aux_status(const void* d_aux, void* stream, uint32_t* status_out);
 
+/* What the synchronisation of the last decode in d_aux cost, beside the
+ * decode's own bytes.  The reference's counterpart is its phase-2 seam
+ * passes (src/multians_gpu_decoder.cu:363-466, 617-656), which re-decode
+ * subsequences until every seam agrees; here merge walks re-decode units
+ * past each region's end until two trajectories meet.  Pass the arguments
+ * of that decode (cfg as given to mans_decode, the workspace size it saw);
+ * the call waits for `stream` and reads the workspace back. */
+typedef struct {
+    uint64_t regions;          /* regions of the plan the decode ran with */
+    uint64_t blocks;           /* blocks of that plan */
+    uint64_t walks;            /* merge walks (regions that have a successor) */
+    uint64_t open_walks;       /* walks the decode pass left to the walk pass */
+    uint64_t walk_units;       /* units the merge walks decoded a second time */
+    uint64_t walk_max_units;   /* units of the longest walk */
+    uint64_t walk_blocks;      /* block starts the walks crossed (walk records) */
+    uint64_t metadata_bytes;   /* block records, walk records, per-region values and
+                                  walk jobs written by the sync passes */
+    uint64_t fallback_warps;   /* symbol capture: warps the final pass decoded */
+    uint32_t unmerged;         /* walks that reached the stream end without merging
+                                  (or ran out of walk slots: MANS_DEV_SYNC_OVERFLOW,
+                                  counted to the stream end) */
+    uint32_t reserved;
+} mans_sync_stats;
+
+int mans_sync_stats_get(const void* d_aux, size_t aux_bytes, size_t n_units, size_t n_out,
+                        uint32_t L, const mans_cfg* cfg, void* stream,
+                        mans_sync_stats* out);
+
 /* Synchronous decode: mans_decode, then the status check; on a sync-walk
  * overflow it re-plans with four times longer regions and decodes again.
  * hint may be NULL. */

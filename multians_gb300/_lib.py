@@ -42,6 +42,13 @@ DECODE_NO_CAPTURE = 0x2
 DECODE_CAPTURE = 0x4
 
 
+class SyncStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "regions", "blocks", "walks", "open_walks", "walk_units", "walk_max_units",
+        "walk_blocks", "metadata_bytes", "fallback_warps")] + [
+        ("unmerged", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
 class Cfg(ctypes.Structure):
     _fields_ = [("block_units", ctypes.c_uint32), ("region_blocks", ctypes.c_uint32),
                 ("walk_slots", ctypes.c_uint32), ("threads", ctypes.c_uint32),
@@ -77,6 +84,8 @@ SIGNATURES = {
     "mans_aux_free": (ctypes.c_int, [_vp]),
     "mans_table_upload": (ctypes.c_int, [_u32p, _u32, ctypes.POINTER(_vp)]),
     "mans_table_free": (ctypes.c_int, [_vp]),
+    "mans_sync_stats_get": (ctypes.c_int, [_vp, _sz, _sz, _sz, _u32, ctypes.POINTER(Cfg), _vp,
+                                           ctypes.POINTER(SyncStats)]),
 }
 
 _lib = None
@@ -131,6 +140,20 @@ def table_check(table) -> int:
     import numpy as np
     t = np.ascontiguousarray(table, dtype=np.uint32)
     return int(lib().mans_table_check(t.ctypes.data_as(_u32p), t.size))
+
+
+def sync_stats(d_aux: int, aux_bytes: int, n_units: int, n_out: int, L: int,
+               cfg: dict | None = None, stream: int | None = None) -> dict:
+    """What the synchronisation of the last decode in the workspace at
+    d_aux cost (mans_sync_stats_get): merge-walk units decoded a second
+    time, the longest walk, walks left to the walk pass, metadata bytes.
+    Pass the decode's own arguments; waits for `stream`."""
+    c = Cfg(**cfg) if cfg else None
+    out = SyncStats()
+    check(lib().mans_sync_stats_get(d_aux, aux_bytes, n_units, n_out, L,
+                                    ctypes.byref(c) if c is not None else None, stream,
+                                    ctypes.byref(out)), "mans_sync_stats_get")
+    return {f: int(getattr(out, f)) for f, _ in SyncStats._fields_ if f != "reserved"}
 
 
 KERNELS = ("k_prep", "k_gwalk", "k_wwalk", "k_scan", "k_final")

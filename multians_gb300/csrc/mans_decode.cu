@@ -1766,6 +1766,24 @@ int mans_table_check(const uint32_t* t, uint32_t L) {
     return loops == (int) L ? 1 : -1;
 }
 
+// The plan a decode with these arguments runs with: the planner's, or the
+// same without symbol capture when capture was the planner's choice and
+// its slices do not fit the workspace (a workspace of mans_aux_size_max
+// bytes always suffices then).
+static int resolve_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* cfg_in,
+                        size_t aux_bytes, mans_cfg* cfg) {
+    int rc = mans_plan(n_units, n_out, L, cfg_in, cfg);
+    if (rc != MANS_OK) return rc;
+    if (cfg->capture_bytes && !(cfg_in && cfg_in->capture_bytes) &&
+        mans_aux_size(n_units, cfg) > aux_bytes) {
+        mans_cfg h = cfg_in ? *cfg_in : mans_cfg{0, 0, 0, 0, 0, 0};
+        h.flags |= MANS_DECODE_NO_CAPTURE;
+        h.capture_bytes = 0;
+        rc = mans_plan(n_units, n_out, L, &h, cfg);
+    }
+    return rc;
+}
+
 int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
                 size_t n_out, const uint32_t* d_table, uint32_t L,
                 uint32_t first_state, uint32_t first_bit, void* d_aux,
@@ -1778,18 +1796,8 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
         first_state >= 2 * L || first_bit > 32 || L > kMaxStates)
         return MANS_ERR_ARG;
     mans_cfg cfg;
-    int rc = mans_plan(n_units, n_out, L, cfg_in, &cfg);
+    int rc = resolve_plan(n_units, n_out, L, cfg_in, aux_bytes, &cfg);
     if (rc != MANS_OK) return rc;
-    if (cfg.capture_bytes && !(cfg_in && cfg_in->capture_bytes) &&
-        mans_aux_size(n_units, &cfg) > aux_bytes) {
-        // capture was the planner's choice and does not fit: decode without
-        // it (a workspace of mans_aux_size_max bytes always suffices then)
-        mans_cfg h = cfg_in ? *cfg_in : mans_cfg{0, 0, 0, 0, 0, 0};
-        h.flags |= MANS_DECODE_NO_CAPTURE;
-        h.capture_bytes = 0;
-        rc = mans_plan(n_units, n_out, L, &h, &cfg);
-        if (rc != MANS_OK) return rc;
-    }
     const size_t nblk = num_blocks(n_units, cfg.block_units);
     const size_t nreg = (nblk + cfg.region_blocks - 1) / cfg.region_blocks;
     const AuxLayout lay = layout_for(nblk, nreg, cfg.walk_slots, cfg.capture_bytes);
@@ -1949,6 +1957,64 @@ int mans_aux_status(const void* d_aux, void* stream, uint32_t* status_out) {
         return MANS_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return MANS_ERR_CUDA;
     *status_out = v;
+    return MANS_OK;
+}
+
+int mans_sync_stats_get(const void* d_aux, size_t aux_bytes, size_t n_units, size_t n_out,
+                        uint32_t L, const mans_cfg* cfg_in, void* stream,
+                        mans_sync_stats* out) {
+    if (!d_aux || !out || n_units == 0 || n_units > 0xffffffffull || n_out == 0 || L < 2 ||
+        L > kMaxStates)
+        return MANS_ERR_ARG;
+    mans_cfg cfg;
+    int rc = resolve_plan(n_units, n_out, L, cfg_in, aux_bytes, &cfg);
+    if (rc != MANS_OK) return rc;
+    const size_t nblk = num_blocks(n_units, cfg.block_units);
+    const size_t nreg = (nblk + cfg.region_blocks - 1) / cfg.region_blocks;
+    const AuxLayout lay = layout_for(nblk, nreg, cfg.walk_slots, cfg.capture_bytes);
+    if (aux_bytes < lay.total) return MANS_ERR_AUX_SMALL;
+    const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
+    // the merge point of every region and the counters behind the scan
+    // flags (flags, ticket, job count, next job, fallback warp count): all
+    // inside the workspace whose size was checked above
+    std::vector<unsigned long long> m(nreg);
+    uint32_t cnt[4] = {0, 0, 0, 0};
+    cudaStream_t st = (cudaStream_t) stream;
+    const char* base = (const char*) d_aux;
+    if (cudaMemcpyAsync(m.data(), base + lay.m, nreg * 8, cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(cnt, base + lay.scan_flags + ntiles * 4, sizeof(cnt),
+                        cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return MANS_ERR_CUDA;
+    const uint64_t bbits = (uint64_t) cfg.block_units * 32;
+    const uint64_t rbits = bbits * cfg.region_blocks;
+    const uint64_t end_bit = (uint64_t) n_units * 32;
+    mans_sync_stats s{};
+    s.regions = nreg;
+    s.blocks = nblk;
+    s.walks = nreg > 0 ? nreg - 1 : 0;
+    s.open_walks = cnt[1];
+    s.fallback_warps = cfg.capture_bytes ? cnt[3] : 0;
+    uint64_t walk_bits = 0;
+    for (size_t k = 0; k + 1 < nreg; ++k) {
+        // region k's walk starts at the first bit of region k + 1 and ends
+        // at the merge point (or at the stream end when it never merged)
+        const uint64_t start = (uint64_t) (k + 1) * rbits;
+        uint64_t stop = m[k];
+        if (stop == ~0ull) {
+            ++s.unmerged;
+            stop = std::max(start, end_bit);
+        }
+        const uint64_t bits = stop > start ? stop - start : 0;
+        walk_bits += bits;
+        s.walk_max_units = std::max<uint64_t>(s.walk_max_units, (bits + 31) / 32);
+        s.walk_blocks += (bits + bbits - 1) / bbits;
+    }
+    s.walk_units = (walk_bits + 31) / 32;
+    s.metadata_bytes = nblk * sizeof(uint2) + s.walk_blocks * sizeof(uint2) + nreg * 4 * 8 +
+                       s.open_walks * sizeof(WJob);
+    *out = s;
     return MANS_OK;
 }
 

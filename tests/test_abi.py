@@ -153,3 +153,28 @@ def test_plan_invariants(mg, L):
                 if R < 4096:   # not clamped by the longest region
                     assert nreg <= lanes_capture[L], (nreg, p)
             assert mg.aux_size(n_units, p) > 0
+
+
+def test_sync_stats_argument_checks(mg):
+    """mans_sync_stats_get refuses bad arguments and a workspace smaller
+    than the plan's before it touches the device (no GPU needed)."""
+    lib = mg.lib()
+    from multians_gb300._lib import SyncStats, Cfg
+    import ctypes
+    out = SyncStats()
+    n_units, n_out, L = 50_000, 260_000, 1024
+    plan = Cfg(**mg.plan(n_units, n_out, L))
+    fake = ctypes.c_void_p(0x100000)   # never dereferenced: every case fails first
+    assert lib.mans_sync_stats_get(None, 1 << 30, n_units, n_out, L, ctypes.byref(plan), None,
+                                   ctypes.byref(out)) == mg.Status.ERR_ARG
+    assert lib.mans_sync_stats_get(fake, 1 << 30, 0, n_out, L, ctypes.byref(plan), None,
+                                   ctypes.byref(out)) == mg.Status.ERR_ARG
+    assert lib.mans_sync_stats_get(fake, 1 << 30, n_units, 0, L, ctypes.byref(plan), None,
+                                   ctypes.byref(out)) == mg.Status.ERR_ARG
+    assert lib.mans_sync_stats_get(fake, 1 << 30, n_units, n_out, 1, ctypes.byref(plan), None,
+                                   ctypes.byref(out)) == mg.Status.ERR_ARG
+    assert lib.mans_sync_stats_get(fake, 1 << 30, n_units, n_out, L, ctypes.byref(plan), None,
+                                   None) == mg.Status.ERR_ARG
+    need = mg.aux_size(n_units, mg.plan(n_units, n_out, L))
+    assert lib.mans_sync_stats_get(fake, need - 256, n_units, n_out, L, ctypes.byref(plan), None,
+                                   ctypes.byref(out)) == mg.Status.ERR_AUX_SMALL
