@@ -170,6 +170,35 @@ def make_workload(args, rank):
     return st, time.time() - t0
 
 
+def profile_figures(workload: str, captured: bool):
+    """The committed ncu figures of a plain workload (profiles/): the kernel
+    each timing slot of the decode stands for (with symbol capture the
+    final-pass slot is the copy pass), DRAM bytes per launch and instruction
+    issue utilisation (% of cycles) by kernel.  Rows are keyed by kernel,
+    workload and capture mode; where no profile of that workload and mode
+    is committed the dictionaries are empty (the bench line then says null,
+    not another kernel's figure)."""
+    key = workload + (" capture" if captured else " no-capture")
+    kernel_of = ({"k_gwalk": "k_gwalk<1>", "k_wwalk": "k_wwalk<1>", "k_final": "k_copy<0>"}
+                 if captured else
+                 {"k_gwalk": "k_gwalk<0>", "k_wwalk": "k_wwalk<0>", "k_final": "k_final<0>"})
+
+    def rows(name):
+        out = {}
+        path = os.path.join(ROOT, "profiles", name)
+        if os.path.exists(path):
+            with open(path) as f:
+                for ln in f:
+                    parts = ln.rstrip("\n").split("\t")
+                    if len(parts) == 3 and not parts[0].startswith("#") and parts[1] == key:
+                        out[parts[0]] = parts[2]
+        return out
+
+    traffic = {k: int(v) for k, v in rows("traffic_per_launch.txt").items()}
+    issue = {k: float(v) for k, v in rows("issue_per_kernel.txt").items()}
+    return kernel_of, traffic, issue
+
+
 def cpu_baseline(st, sample_mb: float):
     """The reference's multicore method (oracle port; the reference build
     when present) on a bounded prefix-sized sample of the same workload."""
@@ -414,26 +443,9 @@ def run_ours(args, ws, rank, local):
     alg = {"k_gwalk": comp_bytes, "k_wwalk": 0, "k_final": n if captured else comp_bytes + n,
            "k_prep": st.L * 4, "k_scan": 0}[dom]
     achieved = alg / (mean_k[dom] / 1e3) / 1e9
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
     wl = f"plain {args.mb:g}MiB lambda={args.lam} L={args.L}"
-    if os.path.exists(tf):
-        with open(tf) as f:
-            for ln in f:
-                parts = ln.strip().split("\t")
-                if len(parts) == 3 and parts[0] == dom and parts[1] == wl:
-                    traffic = int(parts[2])
-    # instruction-issue utilisation of the kernels (ncu, issue active per
-    # scheduler, from the committed profile of this workload): the decode is
-    # bound by issue, not by HBM
-    issue = {}
-    isf = os.path.join(ROOT, "profiles", "issue_per_kernel.txt")
-    if os.path.exists(isf):
-        with open(isf) as f:
-            for ln in f:
-                parts = ln.strip().split("\t")
-                if len(parts) == 3 and parts[1] == wl:
-                    issue[parts[0]] = float(parts[2])
+    kernel_of, t_rows, issue = profile_figures(wl, captured)
+    traffic = t_rows.get(kernel_of.get(dom))
     per_sorted = sorted(per_ms)
     cpu = None
     if not args.no_cpu_baseline:
@@ -458,11 +470,12 @@ def run_ours(args, ws, rank, local):
                             "frac_of_8tbs": round((comp_bytes + n) / (ms / 1e3) / 1e9 / 8000, 4)},
         "kernel_ms": {k: round(v, 4) for k, v in mean_k.items()},
         "sync": sync,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2),
+        "roofline": {"bound": "hbm", "kernel": kernel_of.get(dom, dom),
+                     "timing_slot": dom, "achieved": round(achieved, 2),
                      "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
                      "frac": round(achieved / hbm, 4), "traffic": traffic,
                      "alg_bytes_per_launch": alg},
-        "issue_roofline": {"issue_active_pct": issue, "dominant": dom,
+        "issue_roofline": {"issue_active_pct": issue, "dominant": kernel_of.get(dom, dom),
                            "source": "ncu smsp__issue_active (profiles/)"} if issue else None,
         "cpu_baseline": cpu,
         "e2e": {"value": round(replica_rate(n, ws, e2e_ms), 3), "unit": "GB/s",
