@@ -97,6 +97,12 @@ static uint64_t mt64_next(mt64_t* g) {
     return y;
 }
 
+/* The benchmark workloads' symbol generator: mt19937_64(seed), U = ((x >> 11)
+ * + 1) * 2^-53 in (0, 1], symbol min(255, floor(-ln U / lambda)), an
+ * exponential distribution of rate lambda like the reference demo's
+ * (src/main.cc:46-61, which draws through generate_distribution and
+ * generate_test_data instead; this portable form fixes the bytes for any
+ * standard library). */
 void mo_gen_symbols(uint64_t seed, double lambda, uint8_t* out, size_t n) {
     mt64_t g;
     mt64_seed(&g, seed);
@@ -332,6 +338,8 @@ size_t mo_encode(const uint32_t* enc, uint32_t L, uint32_t max_len,
     return size;
 }
 
+/* CUHDOutputBuffer::reverse (src/multians_output_buffer.cc:27-29): the
+ * decoder writes symbols newest first. */
 void mo_reverse_bytes(uint8_t* buf, size_t n) {
     for (size_t i = 0, j = n ? n - 1 : 0; i < j; ++i, --j) {
         uint8_t t = buf[i];
