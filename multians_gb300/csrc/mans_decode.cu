@@ -343,9 +343,10 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
         __syncwarp();
     }
 
-    // the pass is bound by instruction issue: a unit load every step beats
-    // a refill branch that some lane of the warp takes on most steps
-    // (measured: capturing 0.430 -> 0.398 ms, uncaptured 0.345 -> 0.310 ms)
+    // a unit load every step (one more shared wavefront) beats a refill
+    // branch that some lane of the warp takes on most steps: the pass runs
+    // near its issue limit as well as its shared-memory limit (measured:
+    // capturing 0.430 -> 0.398 ms, uncaptured 0.345 -> 0.310 ms)
     SCursor A;
     uint32_t ca = 0;
     // the capture rows start on a 4 KB boundary, so a row address is the

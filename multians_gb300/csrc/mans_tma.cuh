@@ -101,9 +101,9 @@ struct UnitSrc {
 // Every step loads the unit a refill would take, next to the table entry
 // and before either is needed.  Loading it only on refilling lanes (a
 // branch some lane of the warp takes on most steps, about a fifth of the
-// unit wavefronts) was measured slower in every pass on GB300: the passes
-// are bound by instruction issue or by the walk chain, not by shared-memory
-// wavefronts (G pass 0.345 -> 0.310 ms, final pass 0.349 -> 0.339 ms).
+// unit wavefronts) was measured slower in every pass on GB300: the
+// branch-free step saves more issue slots than the extra wavefronts cost
+// (G pass 0.345 -> 0.310 ms, final pass 0.349 -> 0.339 ms).
 struct SCursor {
     uint2 e;         // table entry of the current state
     uint32_t a;      // shared address of that entry
