@@ -21,6 +21,12 @@ seeded synthetic uint8 symbols, the reference's table generator and encoder
           region), against the measured HBM copy bandwidth.
   cpu_baseline  the reference's multicore CPU method on the host cores, on
           a bounded sample of the same workload.
+  issue_roofline  each kernel's instruction-issue utilisation from the
+          committed ncu summary of this workload (profiles/).
+  sync    what the synchronisation cost beside the algorithmic bytes:
+          units the merge walks decoded a second time, walks handed to the
+          walk pass, metadata bytes (read back from the workspace after the
+          correctness decode, outside the timed region).
 
 Multi-GPU: the decode of one stream does not shard across processes here;
 every rank decodes its own replica stream ("replicas only", weak scaling)
