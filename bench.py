@@ -217,7 +217,7 @@ def cpu_baseline(st, sample_mb: float):
     T = max(1, min(cores, nsub))
     use_ref = O.ref_available()
     times = []
-    for _ in range(3):
+    for _ in range(5):
         t0 = time.perf_counter()
         if use_ref:
             out = O.ref_multicore_decode(sst, S=4, T=T)
@@ -229,7 +229,7 @@ def cpu_baseline(st, sample_mb: float):
     return {"value": round(n / t / 1e9, 4), "unit": "GB/s", "cores": T,
             "kind": "reference" if use_ref else "port",
             "sample": f"{n >> 20} MiB prefix of the workload's symbols, re-encoded; "
-                      f"MulticoreDecoder method S=4, T={T}; median of 3; bit-exact={ok}"}
+                      f"MulticoreDecoder method S=4, T={T}; median of 5; bit-exact={ok}"}
 
 
 def run_reference(args, ws, rank):
