@@ -15,7 +15,7 @@ def sha(a) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-@pytest.mark.parametrize("L", [1024, 4096])
+@pytest.mark.parametrize("L", [256, 1024, 2048, 4096, 8192])
 @pytest.mark.parametrize("lam", [0.005, 0.05, 0.2, 1.0, 2.0])
 def test_library_encoder_matches_oracle(mg, oracle_lib, L, lam):
     from multians_gb300 import host

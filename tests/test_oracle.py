@@ -95,7 +95,7 @@ def test_single_symbol_multicore_reports(oracle_lib):
 
 
 @pytest.mark.parametrize("lam", [0.005, 0.05, 0.2, 1.0, 2.0])
-@pytest.mark.parametrize("L", [1024, 4096])
+@pytest.mark.parametrize("L", [256, 1024, 2048, 4096, 8192])
 def test_oracle_vs_reference_build(oracle_lib, lam, L):
     O = oracle_lib
     if not O.ref_available():
