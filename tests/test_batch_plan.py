@@ -64,3 +64,16 @@ def test_batch_plans_one_stream_like_plain(mg):
         slices, _, _ = _sizes(mg, batch, _descs(batch, [(n_units, n_out, L)]))
         plain = mg.aux_size(n_units, mg.plan(n_units, n_out, L))
         assert abs(slices[0] - plain) <= 256, (slices[0], plain)
+
+
+def test_batch_slices_cover_edge_streams(mg):
+    """The same bound for streams at the edges of the planner: one unit,
+    one symbol, extreme compression ratios (zero-bit runs: many symbols per
+    unit; 8+ bits per symbol), every table size, and an empty output."""
+    from multians_gb300 import batch
+    specs = [(1, 1, 1024), (1, 40, 4096), (4, 1, 256), (2, 512, 8192),
+             (1_000, 400_000, 4096), (1_000, 3_000, 1024), (70_000, 260_000, 2048),
+             (5_000_000, 20_000_000, 1024), (3, 0, 1024), (17, 33, 8192)]
+    slices, hdr, whole = _sizes(mg, batch, _descs(batch, specs))
+    assert whole - hdr <= sum(slices)
+    assert all(s > 0 for s, (_, n_out, _) in zip(slices, specs) if n_out)
