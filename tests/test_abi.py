@@ -178,3 +178,16 @@ def test_sync_stats_argument_checks(mg):
     need = mg.aux_size(n_units, mg.plan(n_units, n_out, L))
     assert lib.mans_sync_stats_get(fake, need - 256, n_units, n_out, L, ctypes.byref(plan), None,
                                    ctypes.byref(out)) == mg.Status.ERR_AUX_SMALL
+
+
+def test_aux_size_max_covers_every_uncaptured_plan(mg):
+    """mans_aux_size_max(n_units) is enough for the plan of any output size
+    and table size without capture (what CUHDGPUDecoderMemory allocates
+    before it sees the output size)."""
+    for n_units in (1, 3, 17, 1000, 65_537, 1 << 20, 12_732_195, 50_339_428, 577_000_000):
+        cap = mg.aux_size_max(n_units)
+        for sym_per_unit in (0.03, 1.0, 3.7, 5.3, 8.4, 21.0, 48.0, 200.0):
+            n_out = max(1, int(n_units * sym_per_unit))
+            for L in (2, 256, 1024, 2048, 4096, 8192):
+                p = mg.plan(n_units, n_out, L, {"flags": mg.DECODE_NO_CAPTURE})
+                assert mg.aux_size(n_units, p) <= cap, (n_units, n_out, L, p)
