@@ -1785,16 +1785,23 @@ static int resolve_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg
     return rc;
 }
 
+// The arguments of a decode with output, checked before any CUDA call.
+static bool decode_args_ok(const uint32_t* d_units, size_t n_units, const uint8_t* d_out,
+                           const uint32_t* d_table, uint32_t L, uint32_t first_state,
+                           uint32_t first_bit, const void* d_aux) {
+    return d_units && ((uintptr_t) d_units & 15) == 0 &&   // TMA needs 16-byte alignment
+           d_out && d_table && d_aux && n_units != 0 && n_units <= 0xffffffffull &&
+           L >= 2 && L <= kMaxStates && first_state >= L && first_state < 2 * L &&
+           first_bit <= 32;
+}
+
 int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
                 size_t n_out, const uint32_t* d_table, uint32_t L,
                 uint32_t first_state, uint32_t first_bit, void* d_aux,
                 size_t aux_bytes, const mans_cfg* cfg_in, void* stream) {
     g_last_launches = 0;
     if (n_out == 0) return MANS_OK;
-    if (((uintptr_t) d_units & 15) != 0) return MANS_ERR_ARG;   // TMA needs 16-byte alignment
-    if (!d_units || !d_out || !d_table || !d_aux || n_units == 0 ||
-        n_units > 0xffffffffull || L < 2 || L > 32768 || first_state < L ||
-        first_state >= 2 * L || first_bit > 32 || L > kMaxStates)
+    if (!decode_args_ok(d_units, n_units, d_out, d_table, L, first_state, first_bit, d_aux))
         return MANS_ERR_ARG;
     mans_cfg cfg;
     int rc = resolve_plan(n_units, n_out, L, cfg_in, aux_bytes, &cfg);
@@ -2076,6 +2083,9 @@ int mans_decode_sync(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
                      uint32_t first_state, uint32_t first_bit, void* d_aux,
                      size_t aux_bytes, const mans_cfg* hint, void* stream,
                      uint32_t* status_out) {
+    if (n_out != 0 &&
+        !decode_args_ok(d_units, n_units, d_out, d_table, L, first_state, first_bit, d_aux))
+        return MANS_ERR_ARG;
     mans_cfg c = {0, 0, 0, 0, 0, 0};
     if (hint) c = *hint;
     mans_cfg plan;

@@ -191,3 +191,39 @@ def test_aux_size_max_covers_every_uncaptured_plan(mg):
             for L in (2, 256, 1024, 2048, 4096, 8192):
                 p = mg.plan(n_units, n_out, L, {"flags": mg.DECODE_NO_CAPTURE})
                 assert mg.aux_size(n_units, p) <= cap, (n_units, n_out, L, p)
+
+
+def _bad_decode_args():
+    a = 0x100000   # 16-byte aligned placeholder addresses, never dereferenced
+    good = dict(units=a, n_units=1000, out=a, n_out=5000, table=a, L=1024, first_state=1500,
+                first_bit=7, aux=a, aux_bytes=1 << 30)
+    cases = {
+        "misaligned units": {"units": a + 4},
+        "null units": {"units": None},
+        "null out": {"out": None},
+        "null table": {"table": None},
+        "null aux": {"aux": None},
+        "no units": {"n_units": 0},
+        "too many units": {"n_units": 1 << 32},
+        "L = 1": {"L": 1, "first_state": 1},
+        "L above 8192": {"L": 16384, "first_state": 16384},
+        "first_state below L": {"first_state": 1023},
+        "first_state at 2L": {"first_state": 2048},
+        "first_bit above 32": {"first_bit": 33},
+    }
+    return [(name, {**good, **bad}) for name, bad in cases.items()]
+
+
+@pytest.mark.parametrize("name,args", _bad_decode_args(), ids=[c[0] for c in _bad_decode_args()])
+def test_decode_entry_points_reject_bad_arguments(mg, name, args):
+    """Every malformed argument is refused with MANS_ERR_ARG before any
+    CUDA call, by the asynchronous and the synchronous decode."""
+    import ctypes
+    lib = mg.lib()
+    v = ctypes.c_void_p
+    pos = (v(args["units"]), args["n_units"], v(args["out"]), args["n_out"], v(args["table"]),
+           args["L"], args["first_state"], args["first_bit"], v(args["aux"]), args["aux_bytes"],
+           None, None)
+    assert lib.mans_decode(*pos) == mg.Status.ERR_ARG, name
+    st = ctypes.c_uint32(0)
+    assert lib.mans_decode_sync(*pos, ctypes.byref(st)) == mg.Status.ERR_ARG, name
