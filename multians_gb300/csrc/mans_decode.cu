@@ -2178,7 +2178,7 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
     // A batch finds its parallelism across streams: regions are sized so the
     // whole batch gives about one G-pass wave of lanes (152 SMs x 16 warps),
     // each with a similar number of symbols, but every stream keeps at least
-    // 32 regions, and never below the planner's length for the stream
+    // 128 regions, and never below the planner's length for the stream
     // alone.  Longer regions mean fewer merge walks and fewer walks that
     // cross a whole region.
     double batch_sym = 0;
@@ -2201,8 +2201,8 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
         if (h.region_blocks == 0) {
             const double spu = (double) d[i].n_out / (double) d[i].n_units;
             const uint64_t B = sp.cfg.block_units;
-            // at least a full warp (32 regions) per stream: a G-pass warp
-            // costs its issue slots however few of its lanes have a region
+            // at least a full G-pass CTA (128 regions) per stream: a CTA's
+            // idle warps still hold its slot on the SM
             const uint64_t want = (uint64_t) std::min(
                 {sym_per_lane / std::max(spu, 1e-3), (double) d[i].n_units / kSyncThreads,
                  (double) kBatchRegionMax});
