@@ -77,3 +77,21 @@ def test_batch_slices_cover_edge_streams(mg):
     slices, hdr, whole = _sizes(mg, batch, _descs(batch, specs))
     assert whole - hdr <= sum(slices)
     assert all(s > 0 for s, (_, n_out, _) in zip(slices, specs) if n_out)
+
+
+@pytest.mark.parametrize("field,value", [
+    ("d_units", 0x100004), ("d_units", None), ("d_out", None), ("d_table", None),
+    ("n_units", 0), ("n_units", 1 << 32), ("L", 1), ("L", 16384),
+    ("first_state", 1023), ("first_state", 2048), ("first_bit", 33)])
+def test_batch_refuses_bad_descriptors(mg, field, value):
+    """A malformed stream descriptor fails the whole batch with
+    MANS_ERR_ARG at sizing time, before any device work."""
+    import ctypes
+    from multians_gb300 import batch
+    descs = _descs(batch, [(1000, 5000, 1024), (2000, 9000, 1024)])
+    setattr(descs[1], field, value)
+    batch._sig()
+    arr = (batch.StreamDesc * 2)(*descs)
+    out = ctypes.c_size_t()
+    assert mg.lib().mans_batch_workspace_size(arr, 2, None, ctypes.byref(out)) == \
+        mg.Status.ERR_ARG
