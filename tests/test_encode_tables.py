@@ -28,3 +28,25 @@ def test_compact_table_matches_reference_table(mg, oracle_lib, L, lam):
         assert np.array_equal(k, enc[s, :, 2].astype(np.uint64)), s
         assert np.array_equal(code, enc[s, :, 1].astype(np.uint64)), s
         assert np.array_equal(nxt[idx.astype(np.int64)], enc[s, :, 0]), s
+
+
+@pytest.mark.parametrize("bad", [
+    {"sym": None}, {"sym": 0x100008}, {"blob": None}, {"blob": 0x200002}, {"units": None},
+    {"aux": None}, {"n": 0}, {"L": 1}, {"L": 1000}, {"L": 16384},
+    {"aux_bytes": 16}, {"cap_units": 1}])
+def test_encode_refuses_bad_arguments(mg, bad):
+    """mans_encode refuses malformed arguments (MANS_ERR_ARG) and short
+    workspaces or unit buffers (MANS_ERR_AUX_SMALL) before any device work."""
+    import ctypes
+    from multians_gb300 import encode
+    lib = encode._sig()
+    vp = ctypes.c_void_p
+    n, L = 100_000, 1024
+    a = dict(sym=0x100000, blob=0x200000, units=0x300000, aux=0x400000, n=n, L=L,
+             aux_bytes=1 << 30, cap_units=lib.mans_encode_max_units(n, L))
+    a.update(bad)
+    rc = lib.mans_encode(vp(a["sym"]), a["n"], vp(a["blob"]), a["L"], vp(a["units"]),
+                         a["cap_units"], vp(a["aux"]), a["aux_bytes"], 0, None)
+    want = mg.Status.ERR_AUX_SMALL if {"aux_bytes", "cap_units"} & set(bad) else \
+        mg.Status.ERR_ARG
+    assert rc == want, (bad, rc)
