@@ -177,7 +177,8 @@ def make_workload(args, rank):
 
 
 def profile_figures(workload: str, captured: bool):
-    """The committed ncu figures of a plain workload (profiles/): the kernel
+    """The committed ncu figures of a plain workload (profiles/traffic_*.txt
+    and profiles/issue_*.txt, tab-separated rows): the kernel
     each timing slot of the decode stands for (with symbol capture the
     final-pass slot is the copy pass), DRAM bytes per launch and instruction
     issue utilisation (% of cycles) by kernel.  Rows are keyed by kernel,
@@ -189,19 +190,22 @@ def profile_figures(workload: str, captured: bool):
                  if captured else
                  {"k_gwalk": "k_gwalk<0>", "k_wwalk": "k_wwalk<0>", "k_final": "k_final<0>"})
 
-    def rows(name):
+    def rows(prefix):
         out = {}
-        path = os.path.join(ROOT, "profiles", name)
-        if os.path.exists(path):
-            with open(path) as f:
+        pdir = os.path.join(ROOT, "profiles")
+        names = sorted(os.listdir(pdir)) if os.path.isdir(pdir) else []
+        for name in names:
+            if not (name.startswith(prefix + "_") and name.endswith(".txt")):
+                continue
+            with open(os.path.join(pdir, name)) as f:
                 for ln in f:
                     parts = ln.rstrip("\n").split("\t")
                     if len(parts) == 3 and not parts[0].startswith("#") and parts[1] == key:
                         out[parts[0]] = parts[2]
         return out
 
-    traffic = {k: int(v) for k, v in rows("traffic_per_launch.txt").items()}
-    issue = {k: float(v) for k, v in rows("issue_per_kernel.txt").items()}
+    traffic = {k: int(v) for k, v in rows("traffic").items()}
+    issue = {k: float(v) for k, v in rows("issue").items()}
     return kernel_of, traffic, issue
 
 
