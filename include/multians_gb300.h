@@ -100,6 +100,12 @@ size_t mans_aux_size(size_t n_units, const mans_cfg* cfg);
  * size, which this call does not see). */
 size_t mans_aux_size_max(size_t n_units);
 
+/* Aux bytes that every plan mans_plan can pick for n_units units fits,
+ * symbol capture included, whatever the output size and table size (what
+ * CUHDGPUDecoderMemory::allocate reserves, so that its decode never needs
+ * more memory). */
+size_t mans_aux_size_max_any(size_t n_units);
+
 /* Decodes one stream; asynchronous on `stream`.  Replaces
  * cuhd::CUHDGPUDecoder::decode (include/cuhd_gpu_decoder.h:24-35,
  * src/multians_gpu_decoder.cu:575-687): same inputs (units, table, initial
@@ -406,11 +412,16 @@ int mans_container_parse(const void* buf, size_t size, mans_container_info* info
  * or when device memory is already exhausted): the workspace is a 32 MiB
  * device array inside this library (mans_noalloc_scratch_bytes), held by
  * every GPU that loads the library until exit.  Same arguments and result
- * as mans_decode_sync; streams whose planned workspace exceeds the array
- * (about 6.4 million units at 6 bits/symbol, 1.7 million at 0.67 bits/symbol)
- * get MANS_ERR_AUX_SMALL before any GPU work.  All calls on a device share the array: calls that overlap
- * on the GPU race, so serialise them.  The first call on a device looks up
- * the array's address and should come before any stream capture.
+ * as mans_decode_sync (arguments are checked first: MANS_ERR_ARG).  A stream
+ * is accepted when a plan of it fits the array (the planner's, else without
+ * symbol capture, else with fewer walk slots: about 28 million units at 6
+ * bits/symbol, 7.7 million at 0.67 bits/symbol, L = 1024); larger ones get
+ * MANS_ERR_AUX_SMALL before any GPU work.  All calls on a device share the
+ * array: calls that overlap on the GPU race, so serialise them.  The first
+ * call on a device looks up the array's address (again after the device's
+ * context is re-created) and should come before any stream capture; under
+ * lazy module loading that first call is also what reserves the array, so
+ * a caller that relies on it once memory is exhausted makes one call early.
  * Synchronous on `stream`. */
 int mans_decode_noalloc(const uint32_t* d_units, size_t n_units, uint8_t* d_out, size_t n_out,
                         const uint32_t* d_table, uint32_t L, uint32_t first_state,
