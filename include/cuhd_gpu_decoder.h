@@ -5,8 +5,13 @@
 // the result is in `output`.  On an error it prints and exits like the
 // reference's CUERR; decode_status() is the same call returning the
 // mans_status code instead.  max_codeword_length is unused (as in the
-// reference); preferred_subsequence_size and threads_per_block are
-// planning hints for the block geometry.
+// reference).  preferred_subsequence_size and threads_per_block are
+// accepted and ignored: the geometry (units per block, blocks per region,
+// threads per CTA) is the planner's, keyed on the table size and the
+// compression ratio; the reference's S = 4 / 128-thread geometry would give
+// this decoder blocks of 4 units and 16 B of records per 16 B of input.
+// The decoder memory must have been allocate()d (MANS_ERR_ARG otherwise);
+// the call itself allocates nothing.
 #ifndef CUHD_GPU_DECODER_
 #define CUHD_GPU_DECODER_
 

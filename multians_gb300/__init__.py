@@ -23,6 +23,7 @@ from ._lib import (  # noqa: F401
     plan,
     aux_size,
     aux_size_max,
+    aux_size_max_any,
     table_check,
     version,
 )
@@ -41,6 +42,7 @@ __all__ = [
     "plan",
     "aux_size",
     "aux_size_max",
+    "aux_size_max_any",
     "table_check",
     "version",
     "MansError",

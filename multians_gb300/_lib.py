@@ -70,6 +70,7 @@ SIGNATURES = {
     "mans_plan": (ctypes.c_int, [_sz, _sz, _u32, ctypes.POINTER(Cfg), ctypes.POINTER(Cfg)]),
     "mans_aux_size": (_sz, [_sz, ctypes.POINTER(Cfg)]),
     "mans_aux_size_max": (_sz, [_sz]),
+    "mans_aux_size_max_any": (_sz, [_sz]),
     "mans_table_check": (ctypes.c_int, [_u32p, _u32]),
     "mans_decode": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _u32, _u32, _u32, _vp, _sz,
                                    ctypes.POINTER(Cfg), _vp]),
@@ -133,6 +134,11 @@ def aux_size(n_units: int, cfg: dict) -> int:
 
 def aux_size_max(n_units: int) -> int:
     return int(lib().mans_aux_size_max(n_units))
+
+
+def aux_size_max_any(n_units: int) -> int:
+    """Aux bytes every plan of n_units units fits, symbol capture included."""
+    return int(lib().mans_aux_size_max_any(n_units))
 
 
 def table_check(table) -> int:

@@ -5,6 +5,7 @@
 // (src/multians_gpu_decoder.cu:575-687), all over the C ABI of
 // include/multians_gb300.h.
 #include <cstdio>
+#include <cstring>
 #include <cstdlib>
 #include <iostream>
 
@@ -31,49 +32,72 @@ cuhd::CUHDGPUOutputBuffer::CUHDGPUOutputBuffer(std::shared_ptr<CUHDOutputBuffer>
                                        output_buffer->get_uncompressed_size()),
       output_buffer_(output_buffer) {}
 
+namespace {
+
+size_t sdiv(size_t a, size_t b) { return b ? (a + b - 1) / b : 0; }
+
+}  // namespace
+
 cuhd::CUHDGPUDecoderMemory::CUHDGPUDecoderMemory(size_t num_units, size_t subsequence_size,
                                                  size_t num_threads)
-    : num_units_(num_units), subsequence_size_(subsequence_size), num_threads_(num_threads) {}
+    : num_units_(num_units), subsequence_size_(subsequence_size), num_threads_(num_threads),
+      num_subseq_(sdiv(num_units, subsequence_size ? subsequence_size : 4)),
+      num_blocks_(sdiv(num_subseq_, num_threads ? num_threads : 128)) {}
 
 cuhd::CUHDGPUDecoderMemory::~CUHDGPUDecoderMemory() { free(); }
 
 void cuhd::CUHDGPUDecoderMemory::allocate() {
     if (is_allocated_) return;
-    bytes_ = mans_aux_size_max(num_units_ ? num_units_ : 1);
+    bytes_ = mans_aux_size_max_any(num_units_ ? num_units_ : 1);
     cudaMalloc(&workspace_, bytes_);
     CUERR
+    // the reference's arrays, same shapes (src/multians_gpu_decoder_memory.cc
+    // :25-50): zero-filled sync points and sizes, and the per-sequence sync
+    // flags on the device and in page-locked host memory
+    const size_t ns = num_subseq_ ? num_subseq_ : 1, nb = num_blocks_ ? num_blocks_ : 1;
+    cudaMalloc((void**) &sync_info_, ns * sizeof(CUHDSubsequenceSyncPoint));
+    cudaMemset(sync_info_, 0, ns * sizeof(CUHDSubsequenceSyncPoint));
+    cudaMalloc((void**) &output_sizes_, ns * sizeof(std::uint32_t));
+    cudaMemset(output_sizes_, 0, ns * sizeof(std::uint32_t));
+    cudaMalloc((void**) &synced_device_, nb);
+    cudaMemset(synced_device_, 0, nb);
+    cudaMallocHost((void**) &synced_host_, nb);
+    CUERR
+    std::memset(synced_host_, 0, nb);
     is_allocated_ = true;
 }
 
-void cuhd::CUHDGPUDecoderMemory::reserve(size_t bytes) {
-    allocate();
-    if (bytes <= bytes_) return;
-    void* grown = nullptr;
-    if (cudaMalloc(&grown, bytes) != cudaSuccess) {
-        cudaGetLastError();   // keep the smaller workspace: the decode runs without capture
-        return;
-    }
-    cudaFree(workspace_);
-    workspace_ = grown;
-    bytes_ = bytes;
+void cuhd::CUHDGPUDecoderMemory::mark_synced() {
+    if (is_allocated_) cudaMemset(synced_device_, 1, num_blocks_ ? num_blocks_ : 1);
 }
 
 void cuhd::CUHDGPUDecoderMemory::free() {
     if (!is_allocated_) return;
     cudaFree(workspace_);
+    cudaFree(sync_info_);
+    cudaFree(output_sizes_);
+    cudaFree(synced_device_);
+    cudaFreeHost(synced_host_);
     workspace_ = nullptr;
+    sync_info_ = nullptr;
+    output_sizes_ = nullptr;
+    synced_device_ = nullptr;
+    synced_host_ = nullptr;
     bytes_ = 0;
     is_allocated_ = false;
 }
 
-void cuhd::CUHDGPUDecoderMemory::retrieve_sync_data() {}
-
-cuhd::CUHDSubsequenceSyncPoint* cuhd::CUHDGPUDecoderMemory::get_sync_info() {
-    return reinterpret_cast<cuhd::CUHDSubsequenceSyncPoint*>(workspace_);
+void cuhd::CUHDGPUDecoderMemory::retrieve_sync_data() {
+    if (!is_allocated_) return;
+    cudaMemcpy(synced_host_, synced_device_, num_blocks_ ? num_blocks_ : 1,
+               cudaMemcpyDeviceToHost);
+    CUERR
 }
-std::uint32_t* cuhd::CUHDGPUDecoderMemory::get_output_sizes() { return nullptr; }
-std::uint8_t* cuhd::CUHDGPUDecoderMemory::get_sequence_synced_device() { return nullptr; }
-std::uint8_t* cuhd::CUHDGPUDecoderMemory::get_sequence_synced_host() { return nullptr; }
+
+cuhd::CUHDSubsequenceSyncPoint* cuhd::CUHDGPUDecoderMemory::get_sync_info() { return sync_info_; }
+std::uint32_t* cuhd::CUHDGPUDecoderMemory::get_output_sizes() { return output_sizes_; }
+std::uint8_t* cuhd::CUHDGPUDecoderMemory::get_sequence_synced_device() { return synced_device_; }
+std::uint8_t* cuhd::CUHDGPUDecoderMemory::get_sequence_synced_host() { return synced_host_; }
 
 int cuhd::CUHDGPUDecoder::decode_status(
     std::shared_ptr<cuhd::CUHDGPUInputBuffer> input, size_t input_size,
@@ -83,15 +107,19 @@ int cuhd::CUHDGPUDecoder::decode_status(
     size_t /*max_codeword_length: unused, as in the reference*/,
     size_t /*preferred_subsequence_size*/, size_t /*threads_per_block*/) {
     if (!input || !output || !table || !aux) return MANS_ERR_ARG;
-    aux->allocate();
-    mans_cfg plan;
-    if (input_size && mans_plan(input_size, output_size, number_of_states, nullptr, &plan) == MANS_OK)
-        aux->reserve(mans_aux_size(input_size, &plan));
+    // the reference's decode allocates nothing (src/multians_gpu_decoder.cu
+    // :575-687): the workspace is what allocate() reserved, which every plan
+    // fits; decoder memory that was never allocated is an argument error
+    if (!aux->is_allocated()) return MANS_ERR_ARG;
     uint32_t dev_status = 0;
-    return mans_decode_sync(input->get(), input_size, output->get(), output_size,
-                            reinterpret_cast<const uint32_t*>(table->get()), number_of_states,
-                            initial_state, initial_bit, aux->get_workspace(),
-                            aux->get_workspace_size(), nullptr, nullptr, &dev_status);
+    const int rc = mans_decode_sync(input->get(), input_size, output->get(), output_size,
+                                    reinterpret_cast<const uint32_t*>(table->get()),
+                                    number_of_states, initial_state, initial_bit,
+                                    aux->get_workspace(), aux->get_workspace_size(), nullptr,
+                                    nullptr, &dev_status);
+    // every sequence is synchronised once the decode has returned
+    if (rc == MANS_OK) aux->mark_synced();
+    return rc;
 }
 
 void cuhd::CUHDGPUDecoder::decode(

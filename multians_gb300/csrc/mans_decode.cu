@@ -1750,6 +1750,21 @@ size_t mans_aux_size_max(size_t n_units) {
     return mans_aux_size(n_units, &c);
 }
 
+size_t mans_aux_size_max_any(size_t n_units) {
+    // symbol capture needs at least 2 bits per symbol (at most 16 symbols
+    // per unit) and L <= 4096; the capture slices grow with the output, and
+    // the region length the planner picks with it depends on L
+    size_t best = mans_aux_size_max(n_units);
+    static const double kSymPerUnit[] = {16, 14, 12, 10, 8, 6, 16.0 / 3, 4, 3.2, 8.0 / 3, 2};
+    for (uint32_t L = 2; L <= kCaptureMaxL; L *= 2)
+        for (double spu : kSymPerUnit) {
+            mans_cfg plan;
+            if (mans_plan(n_units, (size_t) (spu * (double) n_units), L, nullptr, &plan) == MANS_OK)
+                best = std::max(best, mans_aux_size(n_units, &plan));
+        }
+    return best;
+}
+
 int mans_table_check(const uint32_t* t, uint32_t L) {
     if (!t || L < 2 || L > 32768) return -1;
     int loops = 0;

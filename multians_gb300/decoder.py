@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import ctypes
 
-from ._lib import Cfg, MansError, Status, check, lib, aux_size_max
+from ._lib import Cfg, MansError, Status, check, lib, aux_size_max, aux_size_max_any
 
 
 def _torch():
@@ -49,8 +49,8 @@ class CUHDGPUDecoderMemory:
     """Decoder scratch memory sized for ``num_units`` units.  The reference
     sizes it by (units, subsequence size, threads per block)
     (src/multians_gpu_decoder_memory.cc:13-19); here the size covers every
-    geometry the planner may choose, so the two hints are kept only for
-    the signature."""
+    geometry the planner may choose, symbol capture included, so a decode
+    never needs more; the two hints are kept only for the signature."""
 
     def __init__(self, num_units: int, subsequence_size: int = 4, num_threads: int = 128,
                  device=None):
@@ -62,22 +62,13 @@ class CUHDGPUDecoderMemory:
 
     @property
     def nbytes(self) -> int:
-        return aux_size_max(max(1, self.num_units))
+        return aux_size_max_any(max(1, self.num_units))
 
     def allocate(self):
         if self.buf is None:
             torch = _torch()
             self.buf = torch.empty(self.nbytes, dtype=torch.uint8,
                                    device=self.device or "cuda")
-        return self
-
-    def reserve(self, nbytes: int):
-        """Grows the workspace to ``nbytes`` (a plan that captures symbols
-        needs room that scales with the output size)."""
-        self.allocate()
-        if self.buf.numel() < nbytes:
-            torch = _torch()
-            self.buf = torch.empty(nbytes, dtype=torch.uint8, device=self.buf.device)
         return self
 
     def free(self):
@@ -97,10 +88,10 @@ class CUHDGPUDecoder:
         of units (CUHDInputBuffer order), ``table`` a CUDA uint32 tensor of
         packed CUHDCodetableItem words, ``output`` a CUDA uint8 tensor.
         Synchronous; returns the device status bits."""
-        del max_codeword_length  # unused by the reference too (.cu:217)
-        from ._lib import aux_size, plan
-        aux.reserve(aux_size(int(input_size), plan(int(input_size), int(output_size),
-                                                   int(number_of_states), {})))
+        # unused by the reference too (.cu:217); the geometry is the planner's
+        del max_codeword_length, preferred_subsequence_size, threads_per_block
+        if aux.get() is None:
+            raise MansError(Status.ERR_ARG, "CUHDGPUDecoder.decode: decoder memory not allocated")
         st = ctypes.c_uint32(0)
         rc = lib().mans_decode_sync(
             _dev_ptr(input, 4 * int(input_size), "input"), int(input_size),

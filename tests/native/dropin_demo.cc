@@ -37,7 +37,17 @@ static bool run_case(double lambda, size_t n, size_t states) {
                                  dec->get_num_entries(), 11, 4, 128);
     g_out->cpy_device_to_host();
     out->reverse();
-    const bool ok = cuhd::CUHDUtil::equals(data->data(), out->get_decompressed_data().get(), n);
+    bool ok = cuhd::CUHDUtil::equals(data->data(), out->get_decompressed_data().get(), n);
+    // the decoder memory's reference arrays exist with the reference's
+    // shapes, and every sequence reads back as synchronised
+    g_mem->retrieve_sync_data();
+    const size_t nseq = (in->get_compressed_size() + 4 * 128 - 1) / (4 * 128);
+    const std::uint8_t* flags = g_mem->get_sequence_synced_host();
+    bool flags_ok = g_mem->get_sync_info() && g_mem->get_output_sizes() &&
+                    g_mem->get_sequence_synced_device() && flags;
+    for (size_t i = 0; flags_ok && i < nseq; ++i) flags_ok = flags[i] == 1;
+    if (!flags_ok) std::printf("sync flags not set\n");
+    ok = ok && flags_ok;
     std::printf("lambda=%.2f L=%zu n=%zu units=%zu %s\n", lambda, states, n,
                 in->get_compressed_size(), ok ? "ok" : "MISMATCH");
     return ok;

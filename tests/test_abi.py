@@ -193,6 +193,21 @@ def test_aux_size_max_covers_every_uncaptured_plan(mg):
                 assert mg.aux_size(n_units, p) <= cap, (n_units, n_out, L, p)
 
 
+def test_aux_size_max_any_covers_every_plan(mg):
+    """mans_aux_size_max_any(n_units) is enough for the planner's own plan
+    (symbol capture included) of any output size and table size: the
+    drop-in decoder memory reserves it at allocate(), so its decode never
+    needs more memory."""
+    for n_units in (1, 17, 65_537, 1 << 20, 16 << 20, 17_000_000, 50_339_428, 200_000_000):
+        cap = mg.aux_size_max_any(n_units)
+        assert cap >= mg.aux_size_max(n_units)
+        for sym_per_unit in (0.03, 1.0, 2.0, 3.7, 5.3, 8.4, 12.0, 15.9, 16.0, 21.0, 200.0):
+            n_out = max(1, int(n_units * sym_per_unit))
+            for L in (2, 256, 512, 1024, 2048, 4096, 8192):
+                p = mg.plan(n_units, n_out, L)
+                assert mg.aux_size(n_units, p) <= cap, (n_units, n_out, L, p)
+
+
 def _bad_decode_args():
     a = 0x100000   # 16-byte aligned placeholder addresses, never dereferenced
     good = dict(units=a, n_units=1000, out=a, n_out=5000, table=a, L=1024, first_state=1500,
