@@ -19,7 +19,6 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libmans_ref.so")
-REF_ROOT = os.environ.get("MANS_REF_ROOT", "/root/reference")
 
 TABLE_SEED = 5  # the demo's SEED (src/main.cc:24) fed to the table generator
 
@@ -31,12 +30,14 @@ _u32 = ctypes.c_uint32
 
 def build(ref: bool | None = None) -> None:
     """Compiles liboracle.so, and libmans_ref.so when the reference sources
-    are present (or when ``ref`` is True)."""
+    are present (or when ``ref`` is True).  Where the reference tree is read
+    from is the recipe's business (oracle/Makefile: MANS_REF_ROOT from the
+    environment, else its own default)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    want_ref = os.path.isdir(os.path.join(REF_ROOT, "src")) if ref is None else ref
-    if want_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={REF_ROOT}"],
-                       check=True)
+    if ref is None:
+        subprocess.run(["make", "-s", "-C", HERE, "ref-auto"], check=True)
+    elif ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
 
 def _ptr(a: np.ndarray, t):
