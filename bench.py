@@ -28,6 +28,14 @@ seeded synthetic uint8 symbols, the reference's table generator and encoder
           walk pass, metadata bytes (read back from the workspace after the
           correctness decode, outside the timed region).
 
+  batched, served  sub-records measured in the same run after the headline
+          (leave them out with --no-subrecords): the 4096-stream batch as
+          one CUDA-graph replay, with a loop of plain decodes launched from
+          C over the same streams beside it (speedup_batched_vs_loop), and
+          the 20 000-request Poisson trace through the serving loop with
+          p50/p99 latency; each with its own e2e, clocks and bit-exact flag.
+          --workload batched|served prints either as the whole line.
+
 Multi-GPU: the decode of one stream does not shard across processes here;
 every rank decodes its own replica stream ("replicas only", weak scaling)
 and value sums the ranks' decoded bytes over the slowest rank's time.
@@ -49,6 +57,15 @@ sys.path.insert(0, ROOT)
 
 METRIC = "decoded GB/s on 1 GB300 (plain vs batched/served) + %HBM roofline; p50/p99; bit-exact"
 HBM_FALLBACK_GBS = 6800.0
+# Speed of the reference's own MulticoreDecoder build relative to the
+# oracle's port of it (which the reference arm times where the reference
+# sources are absent): same machine, same threads, same stream.
+REFERENCE_VS_PORT = {
+    "ratio": round(0.234 / 0.432, 3),
+    "how": "x86 container, 8 threads, 32 MiB of the headline workload (lambda=0.05, L=1024): "
+           "reference build 0.234 GB/s, port 0.432 GB/s; the port is faster, so a ratio "
+           "against the port understates the speed-up over the reference",
+}
 
 
 def parse():
@@ -66,6 +83,8 @@ def parse():
     ap.add_argument("--no-capture", action="store_true",
                     help="decode without symbol capture (MANS_DECODE_NO_CAPTURE)")
     ap.add_argument("--cpu-sample-mb", type=float, default=32.0)
+    ap.add_argument("--no-subrecords", action="store_true",
+                    help="plain workload: leave out the batched and served sub-records")
     ap.add_argument("--rate", type=float, default=0.0,
                     help="served workload: Poisson arrival rate, requests/s (0 = 50000)")
     return ap.parse_args()
@@ -168,6 +187,14 @@ def replica_rate(per_rank, ws, ms):
     return ws * per_rank / (ms / 1e3) / 1e9
 
 
+def workload_config(args, n_symbols, n_units):
+    """The `config` both arms print for the plain workload (identical keys
+    and values, so the two lines can be matched)."""
+    return {"workload": f"plain {args.mb:g}MiB lambda={args.lam} L={args.L}",
+            "n_symbols": int(n_symbols), "n_units": int(n_units), "lambda": args.lam,
+            "L": args.L, "seed": args.seed}
+
+
 def make_workload(args, rank):
     from multians_gb300 import host
     n = int(args.mb * (1 << 20))
@@ -267,9 +294,7 @@ def run_reference(args, ws, rank):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(tot / len(times) * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": f"plain {args.mb:g}MiB lambda={args.lam} L={args.L}",
-                   "n_symbols": st.n, "n_units": st.n_units, "lambda": args.lam, "L": args.L,
-                   "seed": args.seed},
+        "config": workload_config(args, st.n, st.n_units),
         "bit_exact": ok,
         "latency_ms": {"p50": round(times_ms[len(times_ms) // 2], 3),
                        "p99": round(times_ms[min(len(times_ms) - 1, int(0.99 * len(times_ms)))], 3)},
@@ -278,6 +303,8 @@ def run_reference(args, ws, rank):
                          "sample": f"the full workload per step; MulticoreDecoder method S=4, T={T}"},
         "e2e": {"value": round(v, 4), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "reference_vs_port": REFERENCE_VS_PORT if not use_ref else
+        {"ratio": 1.0, "how": "this run timed the reference's own build"},
     }
     print(json.dumps(line), flush=True)
 
@@ -465,11 +492,12 @@ def run_ours(args, ws, rank, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic",
-        "config": {"workload": wl, "n_symbols": n, "n_units": st.n_units,
-                   "compressed_bytes": comp_bytes, "bits_per_symbol": round(st.bits_per_symbol, 4),
-                   "lambda": args.lam, "L": args.L, "seed": args.seed, "geometry": cfg,
-                   "l2": "inputs larger than L2 (stream + output > 129 MB), no flush",
-                   "parallelism": "replicas" if ws > 1 else "single"},
+        "config": workload_config(args, n, st.n_units),
+        "stream": {"compressed_bytes": comp_bytes,
+                   "bits_per_symbol": round(st.bits_per_symbol, 4)},
+        "geometry": cfg,
+        "l2": "inputs larger than L2 (stream + output > 129 MB), no flush",
+        "parallelism": "replicas" if ws > 1 else "single",
         "bit_exact": bit_exact,
         "latency_ms": {"p50": round(per_sorted[len(per_sorted) // 2], 4),
                        "p99": round(per_sorted[min(len(per_sorted) - 1,
@@ -496,9 +524,42 @@ def run_ours(args, ws, rank, local):
         "clocks": clk.summary(),
         "gen_seconds": round(gen_s, 2),
     }
+    if not args.no_subrecords:
+        line.update(subrecords(args, ws, rank, local))
     print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+# keys of a workload line that repeat the headline's and are left out of its
+# sub-record
+_SUB_DROP = ("metric", "n_gpus", "higher_is_better", "scaling", "vs_baseline", "dtype", "data",
+             "warmup")
+
+
+def subrecords(args, ws, rank, local):
+    """The batched (4096 streams) and served (20 000 requests) workloads,
+    measured after the plain headline in the same run, as sub-records of its
+    line.  Every rank runs them (replicas); rank 0 reports."""
+    import torch
+    from multians_gb300 import bench_workloads, serve_bench
+    out = {}
+    for name, fn in (("batched", bench_workloads.measure_batched),
+                     ("served", serve_bench.measure)):
+        torch.cuda.empty_cache()
+        t0 = time.time()
+        try:
+            sub = fn(args, ws, rank, local)
+        except Exception as e:   # a sub-record never costs the headline its line
+            sub = {"error": f"{type(e).__name__}: {e}"}
+        if sub is not None:
+            sub = {k: v for k, v in sub.items() if k not in _SUB_DROP}
+            sub["wall_seconds"] = round(time.time() - t0, 1)
+            out[name] = sub
+    if "batched" in out and "loop_of_plain" in out["batched"]:
+        out["speedup_batched_vs_loop"] = out["batched"]["loop_of_plain"].get(
+            "speedup_batched_vs_loop")
+    return out
 
 
 def main():

@@ -253,6 +253,19 @@ int mans_decode_batch(const mans_stream_desc* streams, uint32_t n, const mans_cf
                       void* d_workspace, size_t workspace_bytes, void* stream,
                       uint32_t* or_status, uint32_t* per_stream);
 
+/* A loop of plain decodes, the way a C caller decodes many streams one at
+ * a time with the reference's call (src/main.cc:111-116 decodes one stream
+ * per CUHDGPUDecoder::decode): mans_decode of streams[i] with the cached
+ * plan plans[i] (from mans_plan; the descriptor's MANS_DECODE_SOURCE_ORDER
+ * is added) in workspace d_aux[i] of aux_bytes[i] bytes, i = 0 .. n-1, in
+ * order on `stream`, asynchronous.  events may be NULL, else n cudaEvent_t
+ * handles (as void*; NULL entries skipped), events[i] recorded after
+ * stream i's decode.  Stops at the first error and returns it.
+ * mans_last_launch_count then gives the kernels of the whole loop. */
+int mans_decode_loop(const mans_stream_desc* streams, uint32_t n, const mans_cfg* plans,
+                     void* const* d_aux, const size_t* aux_bytes, void* stream,
+                     void* const* events);
+
 /* Serving loop.  No counterpart in the reference, whose decode is one
  * blocking call on the default stream (include/cuhd_gpu_decoder.h:22-36).
  * A server owns one device range of budget_bytes (default 16 GiB, capped at

@@ -38,6 +38,10 @@ def _sig():
     L.mans_decode_batch.restype = ctypes.c_int
     L.mans_batch_destroy.argtypes = [vp]
     L.mans_batch_destroy.restype = ctypes.c_int
+    L.mans_decode_loop.argtypes = [ctypes.POINTER(StreamDesc), u32, ctypes.POINTER(Cfg),
+                                   ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_size_t), vp,
+                                   ctypes.POINTER(vp)]
+    L.mans_decode_loop.restype = ctypes.c_int
     return L
 
 
@@ -140,3 +144,31 @@ def decode_batch(descs, hint: dict | None = None, workspace=None, stream=None):
     check(L.mans_decode_batch(arr, n, ctypes.byref(h) if h else None, ws_ptr, ws_bytes, st,
                               ctypes.byref(acc), per), "mans_decode_batch")
     return int(acc.value), [int(x) for x in per]
+
+
+class Loop:
+    """A loop of plain decodes over many streams, launched from C
+    (mans_decode_loop): each stream with its cached plan and its own
+    workspace, one after another on one CUDA stream."""
+
+    def __init__(self, descs, plans, auxes):
+        from .decoder import _dev_ptr
+        self._L = _sig()
+        self.n = len(descs)
+        self._descs = (StreamDesc * self.n)(*descs)
+        self._plans = (Cfg * self.n)(*[Cfg(**p) for p in plans])
+        self._aux = (ctypes.c_void_p * self.n)(*[_dev_ptr(a).value for a in auxes])
+        self._bytes = (ctypes.c_size_t * self.n)(*[a.numel() for a in auxes])
+        self._keep = auxes
+
+    def run(self, stream, events=None) -> int:
+        """Enqueues the loop; ``events`` (torch.cuda.Event, one per stream,
+        already created) are recorded after each stream's decode.  Returns
+        the number of kernels launched."""
+        ev = None
+        if events is not None:
+            ev = (ctypes.c_void_p * self.n)(*[e.cuda_event for e in events])
+        check(self._L.mans_decode_loop(self._descs, self.n, self._plans, self._aux, self._bytes,
+                                       ctypes.c_void_p(stream.cuda_stream), ev),
+              "mans_decode_loop")
+        return int(lib().mans_last_launch_count())

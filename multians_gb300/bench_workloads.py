@@ -4,8 +4,9 @@ batched: 4096 independent streams, sizes log-uniform in [4 KB, 4 MB] of
 uint8 symbols, each with its own lambda ~ U[0.01, 1], its own L = 1024
 table and its own encoding.  value = decoded GB/s of one CUDA-graph replay
 of the batched decode over all streams; the same streams through a loop of
-plain per-stream decodes (mans_decode, asynchronous, one stream) are timed
-beside it.
+plain per-stream decodes launched from C (mans_decode_loop: cached plans,
+one mans_decode per stream, asynchronous, one CUDA stream) are timed beside
+it, with each stream's GPU time.
 """
 from __future__ import annotations
 
@@ -38,12 +39,12 @@ def batched_specs(seed: int, count: int = 4096, lo: float = 4096, hi: float = 4 
     return [(seed * 7919 + i, float(lams[i]), int(sizes[i]), 1024) for i in range(count)]
 
 
-def run_batched(args, ws, rank, local):
+def measure_batched(args, ws, rank, local):
+    """The batched workload's bench line (None on ranks other than 0)."""
     import torch
 
     import multians_gb300 as mg
     from multians_gb300 import batch
-    from multians_gb300.decoder import decode_async
 
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
@@ -111,27 +112,36 @@ def run_batched(args, ws, rank, local):
     _lib.timing_enable(0)
     kernel_ms = {k: round(v / max(1, kern_n), 4) for k, v in kern_ms.items()}
 
-    # loop of plain decodes over the same streams (workspaces allocated up front)
+    # loop of plain decodes over the same streams, launched from C
+    # (mans_decode_loop) the way a C++ caller runs it: plans cached and
+    # workspaces allocated up front, one mans_decode per stream on one stream
     hint = None if cap else {"flags": mg.DECODE_NO_CAPTURE}
     plans = [mg.plan(st.n_units, st.n, st.L, hint) for st in sts]
     auxes = [torch.empty(mg.aux_size(st.n_units, p), dtype=torch.uint8, device=dev)
              for st, p in zip(sts, plans)]
-
-    def loop():
-        for st, u, t, o, p, a in zip(sts, units, tables, outs, plans, auxes):
-            decode_async(u, st.n_units, o, st.n, t, st.L, st.first_state, st.first_bit, a, p,
-                         stream=stream)
-
-    loop()
+    loop = batch.Loop(descs, plans, auxes)
+    loop.run(stream)
     torch.cuda.synchronize(dev)
     l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    lsteps = 2
+    lsteps = 3
     l0.record(stream)
     for _ in range(lsteps):
-        loop()
+        loop_launches = loop.run(stream)
     l1.record(stream)
     torch.cuda.synchronize(dev)
     loop_ms = l0.elapsed_time(l1) / lsteps
+    # per-stream GPU time: an event after each stream's decode (one more run)
+    sev = [torch.cuda.Event(enable_timing=True) for _ in range(len(sts) + 1)]
+    for e in sev:
+        e.record(stream)   # creates the events
+    torch.cuda.synchronize(dev)
+    sev[0].record(stream)
+    loop.run(stream, events=sev[1:])
+    torch.cuda.synchronize(dev)
+    per_stream = np.array([sev[i].elapsed_time(sev[i + 1]) for i in range(len(sts))])
+    loop_ok = all(np.array_equal(o.cpu().numpy()[::-1], st.symbols)
+                  for st, o in zip(sts, outs))
+    del auxes, loop
 
     # e2e: the packed host units -> device, graph decode, all symbols back
     h_out_all = torch.empty(int(oo[-1]), dtype=torch.uint8).pin_memory()
@@ -215,9 +225,10 @@ def run_batched(args, ws, rank, local):
         del d_units2, d_out2, h_out2
     b.close()
     from bench import max_over_ranks, measured_peaks, replica_rate
-    batch_ms, e2e_ms, e2e_serial_ms = max_over_ranks([batch_ms, e2e_ms, e2e_serial_ms], dev)
+    batch_ms, e2e_ms, e2e_serial_ms, loop_ms = max_over_ranks(
+        [batch_ms, e2e_ms, e2e_serial_ms, loop_ms], dev)
     if rank != 0:
-        return
+        return None
     hbm, kind = measured_peaks()
     value = replica_rate(total_sym, ws, batch_ms)
     alg = (total_comp + total_sym) / (batch_ms / 1e3) / 1e9
@@ -237,7 +248,14 @@ def run_batched(args, ws, rank, local):
         "kernel_ms": kernel_ms,
         "loop_of_plain": {"ms": round(loop_ms, 3),
                           "value": round(total_sym / (loop_ms / 1e3) / 1e9, 3),
-                          "speedup_batched_vs_loop": round(loop_ms / batch_ms, 3)},
+                          "speedup_batched_vs_loop": round(loop_ms / batch_ms, 3),
+                          "launched_from": "C (mans_decode_loop: cached plans, one "
+                                           "mans_decode per stream, one CUDA stream)",
+                          "kernels": int(loop_launches), "bit_exact": bool(loop_ok),
+                          "per_stream_ms": {"mean": round(float(per_stream.mean()), 4),
+                                            "p50": round(float(np.median(per_stream)), 4),
+                                            "p99": round(float(np.quantile(per_stream, 0.99)), 4),
+                                            "max": round(float(per_stream.max()), 4)}},
         "roofline": {"bound": "hbm", "kernel": "batched decode (4 kernels)",
                      "achieved": round(alg, 2), "peak": hbm, "peak_kind": kind, "unit": "GB/s",
                      "frac": round(alg / hbm, 4), "traffic": None,
@@ -253,7 +271,13 @@ def run_batched(args, ws, rank, local):
         "clocks": clk.summary(),
         "gen_seconds": round(gen_s, 2),
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_batched(args, ws, rank, local):
+    line = measure_batched(args, ws, rank, local)
+    if line is not None:
+        print(json.dumps(line), flush=True)
 
 
 def run_encode(args, ws, rank, local):

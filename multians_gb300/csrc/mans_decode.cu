@@ -2136,6 +2136,30 @@ int mans_decode_sync(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
 }
 
 
+int mans_decode_loop(const mans_stream_desc* streams, uint32_t n, const mans_cfg* plans,
+                     void* const* d_aux, const size_t* aux_bytes, void* stream,
+                     void* const* events) {
+    if (n && (!streams || !plans || !d_aux || !aux_bytes)) return MANS_ERR_ARG;
+    uint32_t launches = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const mans_stream_desc& d = streams[i];
+        if (d.n_out != 0) {
+            mans_cfg c = plans[i];
+            c.flags |= d.flags & MANS_DECODE_SOURCE_ORDER;
+            const int rc = mans_decode(d.d_units, d.n_units, d.d_out, d.n_out, d.d_table, d.L,
+                                       d.first_state, d.first_bit, d_aux[i], aux_bytes[i], &c,
+                                       stream);
+            if (rc != MANS_OK) return rc;
+            launches += g_last_launches;
+        }
+        if (events && events[i] &&
+            cudaEventRecord((cudaEvent_t) events[i], (cudaStream_t) stream) != cudaSuccess)
+            return MANS_ERR_CUDA;
+    }
+    g_last_launches = launches;
+    return MANS_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Batched decode of many independent streams (one launch of each kernel for
 // the whole batch; see the BatchItem kernels above).

@@ -125,7 +125,8 @@ def _pcts(lat_ns):
             "mean": round(float(s.mean()), 3), "max": round(float(s[-1]), 3)}
 
 
-def run(args, ws, rank, local):
+def measure(args, ws, rank, local):
+    """The served workload's bench line (None on ranks other than 0)."""
     import torch
 
     import multians_gb300 as mg
@@ -218,6 +219,15 @@ def run(args, ws, rank, local):
     all_ok &= bool((status_l == 0).all())
     lat = done_l.astype(np.int64) - arr_l.astype(np.int64)
     lat_bytes = int(sym_bytes[entry_lat].sum())
+    # latency by request size: the sizes span 1 KB .. 64 MB, so the tail is
+    # the large requests' own decode time plus queueing behind them
+    req_sz = sym_bytes[entry_lat]
+    by_size = {}
+    for name, lo, hi in (("<1MB", 0, 1 << 20), ("1-16MB", 1 << 20, 16 << 20),
+                         (">=16MB", 16 << 20, 1 << 62)):
+        sel = (req_sz >= lo) & (req_sz < hi)
+        if sel.any():
+            by_size[name] = dict(_pcts(lat[sel]), requests=int(sel.sum()))
     lat_span = (int(done_l.max()) - int(arr_l.min())) / 1e9
     stats = srv.stats()
     srv.close()
@@ -243,7 +253,7 @@ def run(args, ws, rank, local):
     served_prefix_bps = total_sym / dev_s
 
     if rank != 0:
-        return
+        return None
     from bench import measured_peaks
     hbm, kind = measured_peaks()
     value = ws * total_sym / dev_s / 1e9
@@ -264,7 +274,8 @@ def run(args, ws, rank, local):
         "bit_exact": bool(ok and all_ok), "verified_requests": n_verify,
         "latency_ms": dict(_pcts(lat), load="half the measured e2e capacity",
                            rate_rps=round(lat_rate, 1),
-                           achieved_gbs=round(lat_bytes / lat_span / 1e9, 3)),
+                           achieved_gbs=round(lat_bytes / lat_span / 1e9, 3),
+                           by_request_size=by_size),
         "latency_ms_saturated": dict(_pcts(np.concatenate(sat_lat)), e2e=_pcts(sat_e2e_lat)),
         "loop_of_plain": {"requests": nl, "seconds": round(loop_s, 3),
                           "value": round(loop_bytes / loop_s / 1e9, 3),
@@ -283,5 +294,11 @@ def run(args, ws, rank, local):
         "clocks": clk.summary(),
         "gen_seconds": round(gen_s, 2), "verify_seconds": round(verify_s, 2),
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run(args, ws, rank, local):
+    line = measure(args, ws, rank, local)
+    if line is not None:
+        print(json.dumps(line), flush=True)
 
