@@ -56,6 +56,7 @@
 #include "mans_device.cuh"
 #include "mans_scan.cuh"
 #include "mans_tma.cuh"
+#include "mans_tune_table.h"
 #include "multians_gb300.h"
 
 namespace mans {
@@ -1540,6 +1541,26 @@ static size_t walk_smem(uint32_t L, bool capture) {
            (kWalkThreads / 32) * 8 + (capture ? 16 + (kWalkThreads / 32) * kCapWarpBytes : 0);
 }
 
+// Staging bytes per warp of the final pass: 1.25x the expected symbols of
+// 32 blocks, 16 B rounded (a warp whose range does not fit writes it
+// directly, byte by byte; 1.5x put the batched final pass at two CTAs per
+// SM), and never more than lets `warps` warps and the table fit the final
+// passes' shared-memory opt-in (long blocks at few bits per symbol would
+// otherwise ask for more and the launch would be refused).
+constexpr size_t kFinalSmemMax = 200 * 1024;
+static uint32_t stage_cap_for(double per_unit, uint32_t B, uint32_t L, uint32_t warps) {
+    uint64_t cap = (uint64_t) (per_unit * 32.0 * B * 1.25) + 128;
+    cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
+    const size_t tab = ((size_t) L * 8 + 15) & ~(size_t) 15;
+    const uint32_t tile_bytes = (B + 4) * 4;
+    const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
+    const size_t fixed = (size_t) 32 * tile_stride + 32;
+    const size_t room = (kFinalSmemMax - tab) / std::max<uint32_t>(warps, 1);
+    const uint64_t fit = room >= fixed + 16 ? ((room - fixed) & ~(size_t) 15) : 16;
+    cap = std::min<uint64_t>(cap, fit);
+    return (uint32_t) ((cap + 15) & ~(uint64_t) 15);
+}
+
 // Opts the kernels in to large dynamic shared memory, once per device.
 static void set_kernel_attributes() {
     static std::mutex mu;
@@ -1553,14 +1574,14 @@ static void set_kernel_attributes() {
     cudaFuncSetAttribute(k_gwalk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_wwalk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_wwalk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_final<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_final<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_final_fb<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(k_final_fb<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_final<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinalSmemMax);
+    cudaFuncSetAttribute(k_final<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinalSmemMax);
+    cudaFuncSetAttribute(k_final_fb<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinalSmemMax);
+    cudaFuncSetAttribute(k_final_fb<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinalSmemMax);
     cudaFuncSetAttribute(k_prep_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_gwalk_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_wwalk_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    cudaFuncSetAttribute(k_final_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_final_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, kFinalSmemMax);
     if (dev < 64) done |= 1ull << dev;
 }
 
@@ -1662,17 +1683,29 @@ constexpr double kCaptureMinBits = 2.0;
 constexpr uint32_t kCaptureMaxL = 4096;   // larger tables leave too little shared memory
 constexpr size_t kCaptureMinUnits = 16u << 20;
 
-int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
-              mans_cfg* out) {
+// The planner's choices a measured table entry overrides (see
+// mans_tune_table.h): units per block, the shortest region in mean meeting
+// distances, and symbol capture.
+struct PlanKnobs {
+    uint32_t block_units;
+    double meet_mult;
+    bool capture;
+};
+
+static int plan_core(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
+                     const PlanKnobs* kn, mans_cfg* out) {
     if (!out || n_units == 0 || L < 2 || L > kMaxStates) return MANS_ERR_ARG;
     mans_cfg c = {0, 0, 0, 0, 0, 0};
     if (hint) c = *hint;
     const double sym_per_unit = n_out ? (double) n_out / (double) n_units : 1.0;
     const double bps = 32.0 / std::max(sym_per_unit, 1e-3);
-    const bool capture = !(c.flags & MANS_DECODE_NO_CAPTURE) &&
-                         (c.capture_bytes != 0 ||
-                          (n_out > 0 && L <= kCaptureMaxL && bps >= kCaptureMinBits &&
-                           (n_units >= kCaptureMinUnits || (c.flags & MANS_DECODE_CAPTURE))));
+    const bool capture =
+        !(c.flags & MANS_DECODE_NO_CAPTURE) &&
+        (c.capture_bytes != 0 ||
+         (kn ? (kn->capture && n_out > 0 && L <= kCaptureMaxL)
+             : (n_out > 0 && L <= kCaptureMaxL && bps >= kCaptureMinBits &&
+                (n_units >= kCaptureMinUnits || (c.flags & MANS_DECODE_CAPTURE)))));
+    if (kn && c.block_units == 0) c.block_units = kn->block_units;
     if (!capture) c.capture_bytes = 0;
     if (c.block_units == 0) {
         // about 128 symbols per block
@@ -1705,7 +1738,7 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
         const uint64_t lanes =
             capture ? std::max(capture_lanes(L, kSyncThreads), capture_lanes(L, kSyncThreadsMax))
                     : 152ull * 16 * 32;
-        const uint64_t r_sync = (uint64_t) (3.0 * meet);
+        const uint64_t r_sync = (uint64_t) ((kn ? kn->meet_mult : 3.0) * meet);
         const uint64_t r_max = std::max<uint64_t>(capture ? 4096 : (L <= 1024 ? 512 : 2048), r_sync);
         uint64_t R = (n_units + lanes - 1) / lanes;
         R = std::min<uint64_t>(std::max<uint64_t>(R, std::max<uint64_t>(r_sync, 64)), r_max);
@@ -1730,8 +1763,90 @@ int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
         c.capture_bytes = (uint32_t) std::min(bytes, (double) (1u << 30));
     }
     c.capture_bytes = (c.capture_bytes + 15) & ~15u;
+    // a table plan without capture says so, so that the plan given back as
+    // a hint (its geometry fixed) keeps deciding the same way
+    if (kn && !capture) c.flags |= MANS_DECODE_NO_CAPTURE;
     *out = c;
     return MANS_OK;
+}
+
+
+// The measured table's entry for a decode of this size, table size and
+// compression ratio: the same L (or, inside the table's range of L, the
+// nearest power of two), the same size class (more or less than 32 MiB of
+// symbols), and the nearest bits per symbol (by ratio).  False when the
+// table has none.
+static bool tune_lookup(uint32_t L, double bps, uint64_t n_out, TuneEntry* out) {
+    const uint32_t large = n_out > (32ull << 20) ? 1u : 0u;
+    uint32_t lo = ~0u, hi = 0;
+    for (uint32_t i = 0; i < kTuneCount; ++i) {
+        lo = std::min(lo, kTuneTable[i].L);
+        hi = std::max(hi, kTuneTable[i].L);
+    }
+    if (kTuneCount == 0 || L < lo || L > hi) return false;
+    const double lg = std::log2((double) L);
+    double best = 1e300;
+    bool found = false;
+    for (uint32_t i = 0; i < kTuneCount; ++i) {
+        const TuneEntry& t = kTuneTable[i];
+        if (t.large != large) continue;
+        const double dl = std::fabs(std::log2((double) t.L) - lg);
+        const double db = std::fabs(std::log(std::max(bps, 1e-3) / (double) t.bps));
+        const double d = dl * 100.0 + db;   // L first, then bits per symbol
+        if (d < best) {
+            best = d;
+            *out = t;
+            found = true;
+        }
+    }
+    return found;
+}
+
+int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
+              mans_cfg* out) {
+    if (!out || n_units == 0 || L < 2 || L > kMaxStates) return MANS_ERR_ARG;
+    // the measured table applies when the caller fixes neither the geometry
+    // nor the capture and does not ask for the model
+    const bool free_plan =
+        !hint || (hint->block_units == 0 && hint->region_blocks == 0 &&
+                  hint->capture_bytes == 0 &&
+                  !(hint->flags & (MANS_PLAN_MODEL | MANS_DECODE_NO_CAPTURE | MANS_DECODE_CAPTURE)));
+    TuneEntry t;
+    if (free_plan && n_out > 0 &&
+        tune_lookup(L, 32.0 * (double) n_units / (double) n_out, n_out, &t)) {
+        // capture as measured, from the length on where it pays at all
+        // (the table's streams are 16 MiB and 256 MiB of symbols; shorter
+        // streams of the large class stay below that length)
+        const PlanKnobs kn = {t.block_units, (double) t.meet_mult,
+                              t.capture != 0 && n_units >= kCaptureMinUnits};
+        return plan_core(n_units, n_out, L, hint, &kn, out);
+    }
+    return plan_core(n_units, n_out, L, hint, nullptr, out);
+}
+
+int mans_plan_tuned(size_t n_units, size_t n_out, uint32_t L, uint32_t block_units,
+                    double meet_mult, int capture, mans_cfg* out) {
+    if (!out || n_units == 0 || L < 2 || L > kMaxStates || block_units < 4 ||
+        block_units > kMaxBlockUnits || (block_units & 3) || !(meet_mult > 0.0) ||
+        meet_mult > 64.0)
+        return MANS_ERR_ARG;
+    const PlanKnobs kn = {block_units, meet_mult, capture != 0};
+    return plan_core(n_units, n_out, L, nullptr, &kn, out);
+}
+
+int mans_tune_lookup(uint32_t L, double bits_per_symbol, uint64_t n_out, mans_tune_entry* out) {
+    if (!out) return MANS_ERR_ARG;
+    TuneEntry t;
+    if (!tune_lookup(L, bits_per_symbol, n_out, &t)) return 0;
+    out->L = t.L;
+    out->bits_per_symbol = t.bps;
+    out->large = t.large;
+    out->block_units = t.block_units;
+    out->meet_mult = t.meet_mult;
+    out->capture = t.capture;
+    out->gbps = t.gbps;
+    out->model_gbps = t.model_gbps;
+    return 1;
 }
 
 size_t mans_aux_size(size_t n_units, const mans_cfg* cfg) {
@@ -1869,13 +1984,9 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
         return MANS_ERR_CUDA;
     const size_t smem = ((size_t) L * sizeof(uint2) + 15) & ~(size_t) 15;
     set_kernel_attributes();
-    // staging per warp: 1.25x the expected symbols of 32 blocks, 16 B
-    // rounded (a warp whose range does not fit writes it directly, byte by
-    // byte; 1.5x put the batched final pass at two CTAs per SM)
-    const double per_unit = (double) n_out / (double) n_units;
-    uint64_t cap = (uint64_t) (per_unit * 32.0 * cfg.block_units * 1.25) + 128;
-    cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
-    p.stage_cap = (uint32_t) ((cap + 15) & ~(uint64_t) 15);
+    const uint32_t fthreads = L >= 4096 ? kFinalThreadsWide : kFinalThreads;
+    p.stage_cap = stage_cap_for((double) n_out / (double) n_units, cfg.block_units, L,
+                                std::max(fthreads, kFinalThreads) / 32);
     // G-pass CTAs: 256 threads share a table for L >= 4096; with capture as
     // capture_threads picks
     const uint32_t gthreads =
@@ -1886,7 +1997,6 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     const uint32_t tile_stride = tile_bytes + ((tile_bytes & 127) == 0 ? 16 : 0);
     const size_t per_warp_final = (size_t) 32 * tile_stride + 16 + p.stage_cap + 16;
     const size_t smem_final = smem + (size_t) (kFinalThreads / 32) * per_warp_final;
-    const uint32_t fthreads = L >= 4096 ? kFinalThreadsWide : kFinalThreads;
     const size_t smem_final_p = smem + (size_t) (fthreads / 32) * per_warp_final;
     timing_mark(0, st);
     k_prep<<<1, 1024, (size_t) L * 12, st>>>(p);
@@ -2195,11 +2305,6 @@ static size_t stream_data_bytes(const BatchStreamPlan& sp) {
     return a.total;
 }
 
-static uint32_t stage_cap_for(double per_unit, uint32_t B) {
-    uint64_t cap = (uint64_t) (per_unit * 32.0 * B * 1.25) + 128;
-    cap = std::min<uint64_t>(std::max<uint64_t>(cap, 512), 16384);
-    return (uint32_t) ((cap + 15) & ~(uint64_t) 15);
-}
 
 constexpr uint64_t kBatchRegionMax = 8192;   // units
 
@@ -2235,6 +2340,10 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
         mans_cfg h = {0, 0, 0, 0, 0, 0};
         if (hint) h = *hint;
         h.flags |= d[i].flags & (MANS_DECODE_NO_CAPTURE | MANS_DECODE_CAPTURE);
+        // batches plan each stream with the model: the measured table is
+        // tuned for streams decoded alone (capture lost on batches of short
+        // streams: the capturing G pass holds fewer warps per SM)
+        h.flags |= MANS_PLAN_MODEL;
         int rc = mans_plan(d[i].n_units, d[i].n_out, d[i].L, &h, &sp.cfg);
         if (rc != MANS_OK) return rc;
         if (h.region_blocks == 0) {
@@ -2265,7 +2374,7 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
         sp.flags_off = flag_words;
         flag_words += sp.ntiles + 4;
         sp.stage_cap = stage_cap_for((double) d[i].n_out / (double) d[i].n_units,
-                                     sp.cfg.block_units);
+                                     sp.cfg.block_units, d[i].L, kFinalThreads / 32);
         const int cls = batch_class(d[i].L);
         lay.n_sync += (sp.nreg + kSyncThreads - 1) / kSyncThreads;
         lay.n_sync_c[cls] += (sp.nreg + kSyncThreads - 1) / kSyncThreads;

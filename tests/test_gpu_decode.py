@@ -69,6 +69,20 @@ def test_geometries(mg, oracle_lib, cfg):
     assert np.array_equal(got[::-1], st.symbols)
 
 
+@pytest.mark.parametrize("L", [4096, 8192])
+def test_long_blocks_at_low_bits_per_symbol(mg, oracle_lib, L):
+    """16-unit blocks at 1.5 bits per symbol ask the final pass for large
+    staging buffers; the decoder caps them to what fits its shared memory
+    (a warp whose range does not fit writes it directly) instead of failing
+    the launch."""
+    O = oracle_lib
+    st = O.make_stream(seed=L + 15, lam=1.0, n=400_000, L=L)
+    for cfg in ({"block_units": 16, "flags": mg.DECODE_NO_CAPTURE},
+                {"block_units": 16, "region_blocks": 301, "flags": mg.DECODE_NO_CAPTURE}):
+        got = _gpu_decode(mg, st, cfg=cfg)
+        assert np.array_equal(got[::-1], st.symbols), cfg
+
+
 @pytest.mark.parametrize("L,lam,cfg", [
     (4096, 0.05, {"block_units": 8, "region_blocks": 9, "walk_slots": 12}),
     (4096, 0.5, {"block_units": 4, "region_blocks": 9, "walk_slots": 12}),
