@@ -195,6 +195,14 @@ def workload_config(args, n_symbols, n_units):
             "L": args.L, "seed": args.seed}
 
 
+def planner_report(mg, st, args):
+    """Where the decode's plan came from: the measured table entry the
+    planner used (multians_gb300/tune.py wrote it from GB300 timings), or the
+    model where the table has none or the run fixed the capture."""
+    entry = None if args.no_capture else mg.tune_lookup(st.L, st.bits_per_symbol, st.n)
+    return {"source": "measured table" if entry else "model", "entry": entry}
+
+
 def make_workload(args, rank):
     from multians_gb300 import host
     n = int(args.mb * (1 << 20))
@@ -496,6 +504,7 @@ def run_ours(args, ws, rank, local):
         "stream": {"compressed_bytes": comp_bytes,
                    "bits_per_symbol": round(st.bits_per_symbol, 4)},
         "geometry": cfg,
+        "planner": planner_report(mg, st, args),
         "l2": "inputs larger than L2 (stream + output > 129 MB), no flush",
         "parallelism": "replicas" if ws > 1 else "single",
         "bit_exact": bit_exact,

@@ -84,9 +84,47 @@ typedef struct {
  * short, capture lost: the capturing G pass holds fewer warps per SM). */
 #define MANS_DECODE_CAPTURE 0x4u
 
-/* Fills `out` with the geometry the decoder uses for this call. */
+/* Plan from the analytic model even where the measured table has an
+ * entry (see mans_plan). */
+#define MANS_PLAN_MODEL 0x8u
+
+/* Fills `out` with the geometry the decoder uses for this call: the built-in
+ * autotuner, keyed on the table size L and the compression ratio (bits per
+ * symbol = 32 n_units / n_out).  Where the hint fixes no geometry and no
+ * capture, units per block, the shortest region (in mean merge distances)
+ * and symbol capture (from 16 Mi units on, where it pays at all) come from
+ * the table the tuning tool measured on GB300 (mans_tune_lookup;
+ * multians_gb300/tune.py writes it), the rest from the model; elsewhere,
+ * or with MANS_PLAN_MODEL, all from the model.  The
+ * reference takes these as fixed caller arguments (subsequence size and
+ * threads per block, include/cuhd_gpu_decoder.h:24-35) and leaves its
+ * CUHDUtil::optimal_subsequence_size (src/multians_util.cc:74-86) unused. */
 int mans_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* hint,
               mans_cfg* out);
+
+/* One measured table entry: the decode it was measured on (L, bits per
+ * symbol, large = 256 MiB of symbols rather than 16 MiB) and the choice the
+ * sweep kept, with its decoded GB/s next to the model's plan's. */
+typedef struct {
+    uint32_t L;
+    float bits_per_symbol;
+    uint32_t large;
+    uint32_t block_units;
+    float meet_mult;          /* shortest region in mean merge distances */
+    uint32_t capture;
+    float gbps;
+    float model_gbps;
+} mans_tune_entry;
+
+/* The table entry mans_plan uses for a decode of n_out symbols at this L and
+ * bits per symbol: returns 1 and fills `out`, or 0 where the table has none
+ * (then the model plans). */
+int mans_tune_lookup(uint32_t L, double bits_per_symbol, uint64_t n_out, mans_tune_entry* out);
+
+/* The plan mans_plan makes from a table entry with these values (what the
+ * tuning sweep times for each candidate). */
+int mans_plan_tuned(size_t n_units, size_t n_out, uint32_t L, uint32_t block_units,
+                    double meet_mult, int capture, mans_cfg* out);
 
 /* Bytes of decoder memory ("aux") a decode with this geometry needs.
  * Replaces CUHDGPUDecoderMemory's sizing by (num_units, subsequence size,

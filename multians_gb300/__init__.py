@@ -19,6 +19,9 @@ from ._lib import (  # noqa: F401
     DECODE_SOURCE_ORDER,
     DECODE_NO_CAPTURE,
     DECODE_CAPTURE,
+    PLAN_MODEL,
+    plan_tuned,
+    tune_lookup,
     lib,
     plan,
     aux_size,

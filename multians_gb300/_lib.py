@@ -40,6 +40,18 @@ class MansError(RuntimeError):
 DECODE_SOURCE_ORDER = 0x1
 DECODE_NO_CAPTURE = 0x2
 DECODE_CAPTURE = 0x4
+PLAN_MODEL = 0x8
+
+
+class TuneEntry(ctypes.Structure):
+    _fields_ = [("L", ctypes.c_uint32), ("bits_per_symbol", ctypes.c_float),
+                ("large", ctypes.c_uint32), ("block_units", ctypes.c_uint32),
+                ("meet_mult", ctypes.c_float), ("capture", ctypes.c_uint32),
+                ("gbps", ctypes.c_float), ("model_gbps", ctypes.c_float)]
+
+    def as_dict(self):
+        return {f: (round(float(getattr(self, f)), 4) if t is ctypes.c_float
+                    else int(getattr(self, f))) for f, t in self._fields_}
 
 
 class SyncStats(ctypes.Structure):
@@ -71,6 +83,10 @@ SIGNATURES = {
     "mans_aux_size": (_sz, [_sz, ctypes.POINTER(Cfg)]),
     "mans_aux_size_max": (_sz, [_sz]),
     "mans_aux_size_max_any": (_sz, [_sz]),
+    "mans_plan_tuned": (ctypes.c_int, [_sz, _sz, _u32, _u32, ctypes.c_double, ctypes.c_int,
+                                       ctypes.POINTER(Cfg)]),
+    "mans_tune_lookup": (ctypes.c_int, [_u32, ctypes.c_double, ctypes.c_uint64,
+                                        ctypes.POINTER(TuneEntry)]),
     "mans_table_check": (ctypes.c_int, [_u32p, _u32]),
     "mans_decode": (ctypes.c_int, [_vp, _sz, _vp, _sz, _vp, _u32, _u32, _u32, _vp, _sz,
                                    ctypes.POINTER(Cfg), _vp]),
@@ -125,6 +141,24 @@ def plan(n_units: int, n_out: int, L: int, hint: dict | None = None) -> dict:
     out = Cfg()
     check(lib().mans_plan(n_units, n_out, L, ctypes.byref(h), ctypes.byref(out)), "mans_plan")
     return out.as_dict()
+
+
+def plan_tuned(n_units: int, n_out: int, L: int, block_units: int, meet_mult: float,
+               capture: bool) -> dict:
+    """The plan mans_plan makes from a measured table entry with these values."""
+    out = Cfg()
+    check(lib().mans_plan_tuned(n_units, n_out, L, block_units, meet_mult, int(capture),
+                                ctypes.byref(out)), "mans_plan_tuned")
+    return out.as_dict()
+
+
+def tune_lookup(L: int, bits_per_symbol: float, n_out: int):
+    """The measured table entry mans_plan uses (dict), or None."""
+    e = TuneEntry()
+    rc = lib().mans_tune_lookup(L, bits_per_symbol, n_out, ctypes.byref(e))
+    if rc < 0 or rc > 1:
+        raise MansError(rc, "mans_tune_lookup")
+    return e.as_dict() if rc == 1 else None
 
 
 def aux_size(n_units: int, cfg: dict) -> int:
