@@ -189,6 +189,36 @@ int mans_sync_stats_get(const void* d_aux, size_t aux_bytes, size_t n_units, siz
                         uint32_t L, const mans_cfg* cfg, void* stream,
                         mans_sync_stats* out);
 
+/* Trajectory query: where the decode of (units, first_state, first_bit)
+ * stands at given bit positions.  For each position q (bits from the start
+ * of the units, unit i holding positions 32 i .. 32 i + 31, read LSB first
+ * as the decoder reads them) the decode's first codeword at or after q: its
+ * bit position, the decoder state there and the number of symbols decoded
+ * before it (found = 0 if the decode does not reach q).  Runs the sync
+ * passes of a decode (no output) and one short decode per position from
+ * the owner record of its block.  This is what splitting one stream over
+ * several GPUs needs (multians_gb300/shard.py): a slice's exit state and
+ * symbol count, and where two starts of a slice meet; the reference's
+ * sync-point array holds the same facts per subsequence
+ * (include/cuhd_subsequence_sync_point.h, src/multians_gpu_decoder.cu
+ * :335-353).  n_out_hint: the expected symbol count, used for planning only
+ * (0: 8 per unit).  d_aux: mans_trajectory_aux_size bytes, 256-byte
+ * aligned.  At most 1024 positions.  Synchronous on `stream`; a
+ * single-symbol table returns MANS_ERR_TABLE. */
+typedef struct {
+    uint64_t pos;      /* bit position of the first codeword at or after q */
+    uint32_t state;    /* decoder state there, in [L, 2L) */
+    uint32_t found;
+    uint64_t count;    /* symbols decoded before it */
+} mans_point;
+
+size_t mans_trajectory_aux_size(size_t n_units, size_t n_out_hint, uint32_t L, uint32_t nq);
+int mans_trajectory_query(const uint32_t* d_units, size_t n_units, const uint32_t* d_table,
+                          uint32_t L, uint32_t first_state, uint32_t first_bit,
+                          size_t n_out_hint, void* d_aux, size_t aux_bytes,
+                          const uint64_t* h_pos, uint32_t nq, mans_point* h_out, void* stream,
+                          uint32_t* dev_status);
+
 /* Synchronous decode: mans_decode, then the status check; on a sync-walk
  * overflow it re-plans with four times longer regions and decodes again.
  * hint may be NULL. */

@@ -211,6 +211,7 @@ constexpr uint32_t kSyncThreads = 128;      // batch launches; plain launches us
 constexpr uint32_t kSyncThreadsMax = 256;   // 256 for L >= 4096 (one table per 8 warps)
 constexpr uint32_t kMaxBlockUnits = 16;
 constexpr uint32_t kMaxWalkSlots = 12;
+constexpr uint32_t kMaxQueries = 1024;   // positions per mans_trajectory_query
 
 __device__ __forceinline__ void ring_fill(uint32_t slot_addr, const uint32_t* __restrict__ in,
                                           uint32_t n, uint32_t chunk, uint32_t bar,
@@ -808,6 +809,58 @@ __device__ __forceinline__ bool block_entry(const DecodeParams& p, uint32_t b,
     idx = min(rec.x >> 8, p.L - 1);   // records come from the sync stage; the clamp keeps
     rel = rec.x & 0xffu;              // table addresses in range regardless
     return true;
+}
+
+// Trajectory queries (mans_trajectory_query): for a bit position q, the
+// decode's first codeword at or after q -- its bit position, its state and
+// how many symbols come before it -- from the owner record of q's block and
+// a short decode from the block's entry.  One thread per query, the table
+// read from global memory: a query decodes less than one block.
+struct QueryPoint {
+    unsigned long long pos;
+    uint32_t state;
+    uint32_t found;
+    unsigned long long count;
+};
+
+__global__ void k_query(DecodeParams p, const unsigned long long* __restrict__ q, uint32_t nq,
+                        QueryPoint* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    QueryPoint r = {0, 0, 0, 0};
+    const uint32_t st = *(volatile uint32_t*) p.status;
+    if (!(st & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE | MANS_DEV_SYNC_OVERFLOW |
+                MANS_DEV_SCAN_TIMEOUT))) {
+        const unsigned long long Bbits = (unsigned long long) p.B * 32;
+        const unsigned long long qq = q[i];
+        const uint32_t b = (uint32_t) min(qq / Bbits, (unsigned long long) p.nblk - 1);
+        uint32_t d;
+        uint2 rec;
+        unsigned long long off;
+        if (block_owner(p, b, d, rec, off)) {
+            unsigned long long pos = b * Bbits + (rec.x & 0xffu);
+            uint32_t j = min(rec.x >> 8, p.L - 1);
+            unsigned long long cnt = off;
+            // a block holds at most B * 32 + 17 bit positions, each with
+            // fewer than L codewords: the bound keeps the loop finite
+            const unsigned long long cap = (Bbits + 17) * p.L;
+            for (unsigned long long s = 0; pos < qq && s < cap; ++s) {
+                const uint2 t = p.tab_sym[j];
+                const unsigned long long u = pos >> 5;
+                const uint32_t w0 = u < p.n_units ? __ldg(p.units + u) : 0u;
+                const uint32_t w1 = u + 1 < p.n_units ? __ldg(p.units + u + 1) : 0u;
+                const uint32_t bits = __funnelshift_r(w0, w1, (uint32_t) (pos & 31u));
+                j = min((t.x >> 3) + (bits & t.y & 0xffffu), p.L - 1);
+                pos += (t.y >> 16) & 0xffu;
+                ++cnt;
+            }
+            r.pos = pos;
+            r.state = j + p.L;
+            r.count = cnt;
+            r.found = pos >= qq ? 1u : 0u;
+        }
+    }
+    out[i] = r;
 }
 
 __device__ __forceinline__ void sts128(uint32_t a, uint4 v) {
@@ -1925,13 +1978,17 @@ static bool decode_args_ok(const uint32_t* d_units, size_t n_units, const uint8_
            first_bit <= 32;
 }
 
-int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
-                size_t n_out, const uint32_t* d_table, uint32_t L,
-                uint32_t first_state, uint32_t first_bit, void* d_aux,
-                size_t aux_bytes, const mans_cfg* cfg_in, void* stream) {
+// The decode's launch sequence; with sync_only the final pass is left out
+// (d_out is not used) and the parameters the passes ran with go to *p_out.
+static int decode_impl(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
+                       size_t n_out, const uint32_t* d_table, uint32_t L,
+                       uint32_t first_state, uint32_t first_bit, void* d_aux,
+                       size_t aux_bytes, const mans_cfg* cfg_in, void* stream, bool sync_only,
+                       DecodeParams* p_out) {
     g_last_launches = 0;
     if (n_out == 0) return MANS_OK;
-    if (!decode_args_ok(d_units, n_units, d_out, d_table, L, first_state, first_bit, d_aux))
+    if (!decode_args_ok(d_units, n_units, sync_only ? (const uint8_t*) d_aux : d_out, d_table, L,
+                        first_state, first_bit, d_aux))
         return MANS_ERR_ARG;
     mans_cfg cfg;
     int rc = resolve_plan(n_units, n_out, L, cfg_in, aux_bytes, &cfg);
@@ -2014,6 +2071,11 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     timing_mark(3, st);
     k_scan<<<(unsigned) ntiles, kScanThreads, 0, st>>>(p);
     timing_mark(4, st);
+    if (sync_only) {
+        if (p_out) *p_out = p;
+        g_last_launches = launches;
+        return cudaGetLastError() == cudaSuccess ? MANS_OK : MANS_ERR_CUDA;
+    }
     const unsigned gf = (unsigned) ((nblk + kFinalThreads - 1) / kFinalThreads);
     const bool rev = (p.flags & MANS_DECODE_SOURCE_ORDER) != 0;
     if (capture) {
@@ -2047,6 +2109,97 @@ int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     g_last_launches = launches;
     if (cudaGetLastError() != cudaSuccess) return MANS_ERR_CUDA;
     return MANS_OK;
+}
+
+int mans_decode(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
+                size_t n_out, const uint32_t* d_table, uint32_t L,
+                uint32_t first_state, uint32_t first_bit, void* d_aux,
+                size_t aux_bytes, const mans_cfg* cfg_in, void* stream) {
+    return decode_impl(d_units, n_units, d_out, n_out, d_table, L, first_state, first_bit, d_aux,
+                       aux_bytes, cfg_in, stream, false, nullptr);
+}
+
+// Query buffers after the sync workspace: positions, then results.
+static size_t query_bytes(uint32_t nq) {
+    return align256((size_t) nq * 8) + align256((size_t) nq * sizeof(QueryPoint));
+}
+
+static mans_cfg query_plan_hint() {
+    mans_cfg h = {0, 0, 0, 0, MANS_DECODE_NO_CAPTURE | MANS_PLAN_MODEL, 0};
+    return h;
+}
+
+size_t mans_trajectory_aux_size(size_t n_units, size_t n_out_hint, uint32_t L, uint32_t nq) {
+    if (n_units == 0 || nq == 0 || nq > kMaxQueries) return 0;
+    const size_t n_out = n_out_hint ? n_out_hint : n_units * 8;
+    mans_cfg plan;
+    const mans_cfg h = query_plan_hint();
+    if (mans_plan(n_units, n_out, L, &h, &plan) != MANS_OK) return 0;
+    // re-plans with longer regions need less; the largest of the first plan
+    // and the worst case without capture
+    return std::max(mans_aux_size(n_units, &plan), mans_aux_size_max(n_units)) + query_bytes(nq);
+}
+
+int mans_trajectory_query(const uint32_t* d_units, size_t n_units, const uint32_t* d_table,
+                          uint32_t L, uint32_t first_state, uint32_t first_bit,
+                          size_t n_out_hint, void* d_aux, size_t aux_bytes,
+                          const uint64_t* h_pos, uint32_t nq, mans_point* h_out, void* stream,
+                          uint32_t* dev_status) {
+    if (dev_status) *dev_status = 0;
+    if (!h_pos || !h_out || nq == 0 || nq > kMaxQueries || !d_aux ||
+        aux_bytes < query_bytes(nq) + 256)
+        return MANS_ERR_ARG;
+    if (!decode_args_ok(d_units, n_units, (const uint8_t*) d_aux, d_table, L, first_state,
+                        first_bit, d_aux))
+        return MANS_ERR_ARG;
+    const size_t n_out = n_out_hint ? n_out_hint : n_units * 8;
+    // the sync workspace, then the query buffers (a multiple of 256 bytes)
+    const size_t work_bytes = (aux_bytes - query_bytes(nq)) & ~(size_t) 255;
+    char* qbase = (char*) d_aux + work_bytes;
+    unsigned long long* d_q = (unsigned long long*) qbase;
+    QueryPoint* d_r = (QueryPoint*) (qbase + align256((size_t) nq * 8));
+    cudaStream_t st = (cudaStream_t) stream;
+    mans_cfg c = query_plan_hint();
+    uint32_t status = 0;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        mans_cfg plan;
+        int rc = mans_plan(n_units, n_out, L, &c, &plan);
+        if (rc != MANS_OK) return rc;
+        if (mans_aux_size(n_units, &plan) > work_bytes) {
+            if (plan.walk_slots > 1) { c = plan; c.walk_slots = plan.walk_slots / 2; continue; }
+            return MANS_ERR_AUX_SMALL;
+        }
+        DecodeParams p;
+        rc = decode_impl(d_units, n_units, nullptr, n_out, d_table, L, first_state, first_bit,
+                         d_aux, work_bytes, &plan, stream, true, &p);
+        if (rc != MANS_OK) return rc;
+        if (cudaMemcpyAsync(d_q, h_pos, (size_t) nq * 8, cudaMemcpyHostToDevice, st) !=
+            cudaSuccess)
+            return MANS_ERR_CUDA;
+        k_query<<<(nq + 127) / 128, 128, 0, st>>>(p, d_q, nq, d_r);
+        if (cudaGetLastError() != cudaSuccess) return MANS_ERR_CUDA;
+        rc = mans_aux_status(d_aux, stream, &status);
+        if (rc != MANS_OK) return rc;
+        if (!(status & MANS_DEV_SYNC_OVERFLOW)) {
+            std::vector<QueryPoint> r(nq);
+            if (cudaMemcpy(r.data(), d_r, (size_t) nq * sizeof(QueryPoint),
+                           cudaMemcpyDeviceToHost) != cudaSuccess)
+                return MANS_ERR_CUDA;
+            for (uint32_t i = 0; i < nq; ++i) {
+                h_out[i].pos = r[i].pos;
+                h_out[i].state = r[i].state;
+                h_out[i].found = r[i].found;
+                h_out[i].count = r[i].count;
+            }
+            break;
+        }
+        // a walk outran its slots: longer regions, as the synchronous decode
+        c = plan;
+        c.region_blocks = plan.region_blocks * 4;
+    }
+    if (dev_status) *dev_status = status;
+    if (status & MANS_DEV_DEGENERATE) return MANS_ERR_TABLE;
+    return mans_status_code(status);
 }
 
 int mans_timing_enable(int max_decodes) {
