@@ -88,6 +88,16 @@ typedef struct {
  * entry (see mans_plan). */
 #define MANS_PLAN_MODEL 0x8u
 
+/* Start anywhere: first_bit gives the decode's start as a bit offset from
+ * the least significant bit of the first unit, 0 .. 127, instead of the
+ * reference's count of valid bits in unit 0 (the start at bit
+ * 32 - first_bit).  A decode can then begin at any bit of a stream whose
+ * units it addresses from the 16-byte aligned unit at most 3 units before
+ * the start: a segment of a multi-table stream (multians_gb300/segments.py).
+ * Honoured by mans_decode, mans_decode_sync, the batch descriptors' flags
+ * and mans_trajectory_query. */
+#define MANS_DECODE_START_OFFSET 0x10u
+
 /* Fills `out` with the geometry the decoder uses for this call: the built-in
  * autotuner, keyed on the table size L and the compression ratio (bits per
  * symbol = 32 n_units / n_out).  Where the hint fixes no geometry and no
@@ -202,7 +212,8 @@ int mans_sync_stats_get(const void* d_aux, size_t aux_bytes, size_t n_units, siz
  * sync-point array holds the same facts per subsequence
  * (include/cuhd_subsequence_sync_point.h, src/multians_gpu_decoder.cu
  * :335-353).  n_out_hint: the expected symbol count, used for planning only
- * (0: 8 per unit).  d_aux: mans_trajectory_aux_size bytes, 256-byte
+ * (0: 8 per unit).  flags: MANS_DECODE_START_OFFSET or 0.  d_aux:
+ * mans_trajectory_aux_size bytes, 256-byte
  * aligned.  At most 1024 positions.  Synchronous on `stream`; a
  * single-symbol table returns MANS_ERR_TABLE. */
 typedef struct {
@@ -214,7 +225,7 @@ typedef struct {
 
 size_t mans_trajectory_aux_size(size_t n_units, size_t n_out_hint, uint32_t L, uint32_t nq);
 int mans_trajectory_query(const uint32_t* d_units, size_t n_units, const uint32_t* d_table,
-                          uint32_t L, uint32_t first_state, uint32_t first_bit,
+                          uint32_t L, uint32_t first_state, uint32_t first_bit, uint32_t flags,
                           size_t n_out_hint, void* d_aux, size_t aux_bytes,
                           const uint64_t* h_pos, uint32_t nq, mans_point* h_out, void* stream,
                           uint32_t* dev_status);

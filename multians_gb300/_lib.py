@@ -40,6 +40,7 @@ class MansError(RuntimeError):
 DECODE_SOURCE_ORDER = 0x1
 DECODE_NO_CAPTURE = 0x2
 DECODE_CAPTURE = 0x4
+DECODE_START_OFFSET = 0x10
 PLAN_MODEL = 0x8
 
 

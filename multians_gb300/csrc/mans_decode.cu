@@ -1969,13 +1969,20 @@ static int resolve_plan(size_t n_units, size_t n_out, uint32_t L, const mans_cfg
 }
 
 // The arguments of a decode with output, checked before any CUDA call.
+// first_bit: the reference's count of valid bits in unit 0 (the decode
+// starts at bit 32 - first_bit), or with MANS_DECODE_START_OFFSET the start
+// itself, a bit offset < 128 from the first unit's least significant bit.
 static bool decode_args_ok(const uint32_t* d_units, size_t n_units, const uint8_t* d_out,
                            const uint32_t* d_table, uint32_t L, uint32_t first_state,
-                           uint32_t first_bit, const void* d_aux) {
+                           uint32_t first_bit, const void* d_aux, uint32_t flags = 0) {
     return d_units && ((uintptr_t) d_units & 15) == 0 &&   // TMA needs 16-byte alignment
            d_out && d_table && d_aux && n_units != 0 && n_units <= 0xffffffffull &&
            L >= 2 && L <= kMaxStates && first_state >= L && first_state < 2 * L &&
-           first_bit <= 32;
+           first_bit <= ((flags & MANS_DECODE_START_OFFSET) ? 127u : 32u);
+}
+
+static uint32_t start_pos(uint32_t first_bit, uint32_t flags) {
+    return (flags & MANS_DECODE_START_OFFSET) ? first_bit : 32 - first_bit;
 }
 
 // The decode's launch sequence; with sync_only the final pass is left out
@@ -1987,8 +1994,9 @@ static int decode_impl(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
                        DecodeParams* p_out) {
     g_last_launches = 0;
     if (n_out == 0) return MANS_OK;
+    const uint32_t in_flags = cfg_in ? cfg_in->flags : 0u;
     if (!decode_args_ok(d_units, n_units, sync_only ? (const uint8_t*) d_aux : d_out, d_table, L,
-                        first_state, first_bit, d_aux))
+                        first_state, first_bit, d_aux, in_flags))
         return MANS_ERR_ARG;
     mans_cfg cfg;
     int rc = resolve_plan(n_units, n_out, L, cfg_in, aux_bytes, &cfg);
@@ -2021,7 +2029,7 @@ static int decode_impl(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     p.n_units = (uint32_t) n_units;
     p.L = L;
     p.first_idx = first_state - L;
-    p.first_pos = 32 - first_bit;
+    p.first_pos = start_pos(first_bit, in_flags);
     p.B = cfg.block_units;
     p.nb = cfg.region_blocks;
     p.dmax = cfg.walk_slots;
@@ -2141,7 +2149,7 @@ size_t mans_trajectory_aux_size(size_t n_units, size_t n_out_hint, uint32_t L, u
 }
 
 int mans_trajectory_query(const uint32_t* d_units, size_t n_units, const uint32_t* d_table,
-                          uint32_t L, uint32_t first_state, uint32_t first_bit,
+                          uint32_t L, uint32_t first_state, uint32_t first_bit, uint32_t flags,
                           size_t n_out_hint, void* d_aux, size_t aux_bytes,
                           const uint64_t* h_pos, uint32_t nq, mans_point* h_out, void* stream,
                           uint32_t* dev_status) {
@@ -2149,8 +2157,9 @@ int mans_trajectory_query(const uint32_t* d_units, size_t n_units, const uint32_
     if (!h_pos || !h_out || nq == 0 || nq > kMaxQueries || !d_aux ||
         aux_bytes < query_bytes(nq) + 256)
         return MANS_ERR_ARG;
+    flags &= MANS_DECODE_START_OFFSET;
     if (!decode_args_ok(d_units, n_units, (const uint8_t*) d_aux, d_table, L, first_state,
-                        first_bit, d_aux))
+                        first_bit, d_aux, flags))
         return MANS_ERR_ARG;
     const size_t n_out = n_out_hint ? n_out_hint : n_units * 8;
     // the sync workspace, then the query buffers (a multiple of 256 bytes)
@@ -2160,6 +2169,7 @@ int mans_trajectory_query(const uint32_t* d_units, size_t n_units, const uint32_
     QueryPoint* d_r = (QueryPoint*) (qbase + align256((size_t) nq * 8));
     cudaStream_t st = (cudaStream_t) stream;
     mans_cfg c = query_plan_hint();
+    c.flags |= flags;
     uint32_t status = 0;
     for (int attempt = 0; attempt < 8; ++attempt) {
         mans_cfg plan;
@@ -2196,6 +2206,7 @@ int mans_trajectory_query(const uint32_t* d_units, size_t n_units, const uint32_
         // a walk outran its slots: longer regions, as the synchronous decode
         c = plan;
         c.region_blocks = plan.region_blocks * 4;
+        c.flags |= flags;
     }
     if (dev_status) *dev_status = status;
     if (status & MANS_DEV_DEGENERATE) return MANS_ERR_TABLE;
@@ -2361,8 +2372,8 @@ int mans_decode_sync(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
                      uint32_t first_state, uint32_t first_bit, void* d_aux,
                      size_t aux_bytes, const mans_cfg* hint, void* stream,
                      uint32_t* status_out) {
-    if (n_out != 0 &&
-        !decode_args_ok(d_units, n_units, d_out, d_table, L, first_state, first_bit, d_aux))
+    if (n_out != 0 && !decode_args_ok(d_units, n_units, d_out, d_table, L, first_state,
+                                      first_bit, d_aux, hint ? hint->flags : 0u))
         return MANS_ERR_ARG;
     mans_cfg c = {0, 0, 0, 0, 0, 0};
     if (hint) c = *hint;
@@ -2487,7 +2498,8 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
         if (!sp.active) continue;
         if (!d[i].d_units || !d[i].d_out || !d[i].d_table || d[i].n_units == 0 ||
             d[i].n_units > 0xffffffffull || d[i].L < 2 || d[i].L > kMaxStates ||
-            d[i].first_state < d[i].L || d[i].first_state >= 2 * d[i].L || d[i].first_bit > 32 ||
+            d[i].first_state < d[i].L || d[i].first_state >= 2 * d[i].L ||
+            d[i].first_bit > ((d[i].flags & MANS_DECODE_START_OFFSET) ? 127u : 32u) ||
             ((uintptr_t) d[i].d_units & 15) != 0)
             return MANS_ERR_ARG;
         mans_cfg h = {0, 0, 0, 0, 0, 0};
@@ -2518,7 +2530,7 @@ static int plan_batch(const mans_stream_desc* d, uint32_t n, const mans_cfg* hin
                 if (rc != MANS_OK) return rc;
             }
         }
-        sp.cfg.flags = d[i].flags & MANS_DECODE_SOURCE_ORDER;
+        sp.cfg.flags = d[i].flags & (MANS_DECODE_SOURCE_ORDER | MANS_DECODE_START_OFFSET);
         sp.nblk = num_blocks(d[i].n_units, sp.cfg.block_units);
         sp.nreg = (sp.nblk + sp.cfg.region_blocks - 1) / sp.cfg.region_blocks;
         sp.ntiles = (sp.nreg + kScanTile - 1) / kScanTile;
@@ -2675,7 +2687,7 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         p.n_units = (uint32_t) d.n_units;
         p.L = d.L;
         p.first_idx = d.first_state - d.L;
-        p.first_pos = 32 - d.first_bit;
+        p.first_pos = start_pos(d.first_bit, d.flags);
         p.B = sp.cfg.block_units;
         p.nb = sp.cfg.region_blocks;
         p.dmax = sp.cfg.walk_slots;
@@ -2860,7 +2872,10 @@ int mans_batch_fixup(mans_batch* b, void* stream, uint32_t* n_redone) {
         hint.region_blocks = sp.cfg.region_blocks * 4;   // longer regions, same slots
         uint32_t dev_status = 0;
         const int rc = mans_decode_sync(p.units, p.n_units, p.out, p.n_out, p.table, p.L,
-                                        p.first_idx + p.L, 32 - p.first_pos, slice, slice_bytes,
+                                        p.first_idx + p.L,
+                                        (sp.cfg.flags & MANS_DECODE_START_OFFSET)
+                                            ? p.first_pos : 32 - p.first_pos,
+                                        slice, slice_bytes,
                                         &hint, stream, &dev_status);
         if (rc != MANS_OK && rc != MANS_ERR_SYNC) return rc;
         if (cudaMemcpyAsync(b->base + b->lay.status + 4ull * i, &dev_status, 4,

@@ -91,7 +91,8 @@ class GpuBackend:
         self._lib = lib()
         f = self._lib.mans_trajectory_query
         f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_uint32,
-                      ctypes.c_uint32, ctypes.c_uint32, ctypes.c_size_t, ctypes.c_void_p,
+                      ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_size_t,
+                      ctypes.c_void_p,
                       ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
                       ctypes.POINTER(Point), ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)]
         f.restype = ctypes.c_int
@@ -99,20 +100,23 @@ class GpuBackend:
         g.argtypes = [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint32]
         g.restype = ctypes.c_size_t
 
-    def query(self, state: int, first_bit: int, n_units: int, positions):
+    def query(self, state: int, first_bit: int, n_units: int, positions, flags: int = 0,
+              units=None, table=None):
         import torch
 
         from ._lib import MansError
         from .decoder import _dev_ptr, _stream_ptr
+        units = self.units if units is None else units
+        table = self.table if table is None else table
         nq = len(positions)
         need = self._lib.mans_trajectory_aux_size(n_units, self.n_out_hint, self.L, nq)
-        aux = torch.empty(need, dtype=torch.uint8, device=self.units.device)
+        aux = torch.empty(need, dtype=torch.uint8, device=units.device)
         q = (ctypes.c_uint64 * nq)(*[int(x) for x in positions])
         out = (Point * nq)()
         st = ctypes.c_uint32(0)
         rc = self._lib.mans_trajectory_query(
-            _dev_ptr(self.units, 4 * n_units, "units"), n_units,
-            _dev_ptr(self.table, 4 * self.L, "table"), self.L, int(state), int(first_bit),
+            _dev_ptr(units, 4 * n_units, "units"), n_units,
+            _dev_ptr(table, 4 * self.L, "table"), self.L, int(state), int(first_bit), int(flags),
             self.n_out_hint, _dev_ptr(aux), need, q, nq, out, _stream_ptr(None),
             ctypes.byref(st))
         if rc:
@@ -181,7 +185,8 @@ def decode_sharded(backend, sl: Slice, group=None, prefix_units: int | None = No
             if not 0 <= off < 32:
                 raise RuntimeError(f"rank {sl.rank}: predecessor's exit {off} bits into the slice")
             # 3. the true start of this slice, at the end of the prefix
-            tW = backend.query(state, 32 - off, held, [32 * W])[0]
+            # the true start up to the prefix end only: units past it unread
+            tW = backend.query(state, 32 - off, min(held, W + HALO_UNITS), [32 * W])[0]
             if tW[2] and (tW[0], tW[1]) == (gW[0], gW[1]):
                 new_count, new_exit = tW[3] + gX[3] - gW[3], exit_of(gX)
             else:

@@ -23,6 +23,13 @@
 static inline uint32_t hshl(uint32_t x, uint64_t n) { return x << (n & 31u); }
 static inline uint32_t hshr(uint32_t x, uint64_t n) { return x >> (n & 31u); }
 
+/* Segment of source symbol i (segments in order; seg: the last answer, as
+ * i only grows); past the end, the last segment. */
+static inline size_t seg_of(const size_t* seg_end, size_t n_seg, size_t seg, uint64_t i) {
+    while (seg + 1 < n_seg && i >= seg_end[seg]) ++seg;
+    return seg;
+}
+
 /* ---------------------------------------------------------------------- */
 /* Mersenne Twister generators (Matsumoto & Nishimura 1998; the 64-bit    */
 /* variant of 2004), as std::mt19937 / std::mt19937_64 define them.       */
@@ -338,6 +345,67 @@ size_t mo_encode(const uint32_t* enc, uint32_t L, uint32_t max_len,
     return size;
 }
 
+/* Multi-table streams (the reference names multi-table decoding as future
+ * work, README.md:11, and defines no format for it).  The encoder above
+ * with the encoder table chosen per source symbol by the segment the symbol
+ * belongs to: segment j holds source symbols [seg_end[j-1], seg_end[j]),
+ * all tables have L states, and the state carries over from one segment to
+ * the next, so the stream is one bitstream with one first state and bit.
+ * The look-ahead byte past the end is encoded with the last segment's
+ * table. */
+size_t mo_encode_segments(const uint32_t* const* encs, const size_t* seg_end, size_t n_seg,
+                          uint32_t L, uint32_t max_len, const uint8_t* in, size_t size_in,
+                          uint32_t* units, size_t cap, uint32_t* first_bit,
+                          uint32_t* first_state) {
+    if (n_seg == 0 || seg_end[n_seg - 1] != size_in) return 0;
+    const size_t size_out = mo_max_units(max_len, size_in);
+    uint32_t* out = (uint32_t*) calloc(size_out ? size_out : 1, sizeof(uint32_t));
+    if (!out) return 0;
+    const uint64_t max_bits = 32;
+    size_t seg = 0;
+#define SEG_ENC(i) (encs[(seg = seg_of(seg_end, n_seg, seg, (i)))])
+    uint32_t window = 0, state = 0, final_state = 0;
+    uint64_t final_bit = 0, final_size = 0, at = 0, in_unit = 0;
+
+    for (size_t i = 0; i < size_out && in_unit < size_in + 1; ++i) {
+        const uint32_t* e = SEG_ENC(in_unit) + ((size_t) in[in_unit] * L + state) * 4;
+        state = e[0] - L;
+        uint32_t rem = e[1];
+        uint64_t shift = e[2];
+        while (at + shift < max_bits && in_unit < size_in) {
+            window = hshl(window, shift);
+            window += rem;
+            at += shift;
+            ++in_unit;
+            if (in_unit < size_in) {
+                e = SEG_ENC(in_unit) + ((size_t) in[in_unit] * L + state) * 4;
+                state = e[0] - L;
+                rem = e[1];
+                shift = e[2];
+            }
+            final_state = e[0];
+        }
+        const uint64_t diff = at + shift - max_bits;
+        final_bit = at;
+        final_size = i;
+        window = hshl(window, shift - diff);
+        window += hshr(rem, diff);
+        out[i] = window;
+        window = rem & ~hshl(~0u, diff);
+        at = diff;
+        ++in_unit;
+    }
+#undef SEG_ENC
+    const size_t size = (size_t) final_size + 1;
+    if (size + 4 > cap) { free(out); return 0; }
+    for (size_t i = 0; i < size; ++i) units[i] = out[size - 1 - i];
+    for (size_t i = 0; i < 4; ++i) units[size + i] = 0;
+    *first_bit = (uint32_t) final_bit;
+    *first_state = final_state;
+    free(out);
+    return size;
+}
+
 /* CUHDOutputBuffer::reverse (src/multians_output_buffer.cc:27-29): the
  * decoder writes symbols newest first. */
 void mo_reverse_bytes(uint8_t* buf, size_t n) {
@@ -396,6 +464,35 @@ int mo_decode_seq(const uint32_t* units, size_t n_units, uint32_t first_bit,
             last_p = p;
         }
         if (x < L || x >= 2 * L) return -1;
+    }
+    return 0;
+}
+
+/* Sequential decode of a multi-table stream: counts[j] symbols with
+ * decs[j] for the segments in decode order (the source's last segment
+ * first), the state carried across; starts[j] receives the bit position of
+ * segment j's first codeword. */
+int mo_decode_segments(const uint32_t* units, size_t n_units, uint32_t first_bit,
+                       uint32_t first_state, const uint32_t* const* decs, const size_t* counts,
+                       size_t n_seg, uint32_t L, uint8_t* out, uint64_t* starts) {
+    uint32_t x = first_state;
+    uint64_t p = 32 - (uint64_t) first_bit;
+    size_t o = 0;
+    if (x < L || x >= 2 * L) return -1;
+    for (size_t j = 0; j < n_seg; ++j) {
+        starts[j] = p;
+        uint64_t last_p = p, zero_run = 0;
+        for (size_t i = 0; i < counts[j]; ++i) {
+            uint32_t hit = step(units, n_units, decs[j], L, &x, &p);
+            out[o++] = (uint8_t) (hit >> 16);
+            if (p == last_p) {
+                if (++zero_run > L) return -1;
+            } else {
+                zero_run = 0;
+                last_p = p;
+            }
+            if (x < L || x >= 2 * L) return -1;
+        }
     }
     return 0;
 }

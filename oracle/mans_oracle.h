@@ -63,6 +63,13 @@ int mo_decode_seq(const uint32_t* units, size_t n_units, uint32_t first_bit,
 /* True sync points for subsequences of S units (nsub = ceil(n_units / S)):
  * sp[4*i .. 4*i+3] = {unit, bit, exclusive symbol offset, state}.  The last
  * subsequence is decoded to its end, padding included. Returns 0 / -1. */
+size_t mo_encode_segments(const uint32_t* const* encs, const size_t* seg_end, size_t n_seg,
+                          uint32_t L, uint32_t max_len, const uint8_t* in, size_t size_in,
+                          uint32_t* units, size_t cap, uint32_t* first_bit,
+                          uint32_t* first_state);
+int mo_decode_segments(const uint32_t* units, size_t n_units, uint32_t first_bit,
+                       uint32_t first_state, const uint32_t* const* decs, const size_t* counts,
+                       size_t n_seg, uint32_t L, uint8_t* out, uint64_t* starts);
 int mo_sync_points(size_t S, const uint32_t* units, size_t n_units,
                    uint32_t first_bit, uint32_t first_state,
                    const uint32_t* dec, uint32_t L, uint32_t* sp);

@@ -67,6 +67,14 @@ def lib():
         L.mo_sync_points.argtypes = [_sz, _u32p, _sz, _u32, _u32, _u32p, _u32, _u32p]
         L.mo_sync_points.restype = ctypes.c_int
         L.mo_multicore_decode.argtypes = [_sz, _sz, _u32p, _sz, _u32, _u32, _u32p, _u32, _u8p, _sz]
+        _pp = ctypes.POINTER(_u32p)
+        _szp = ctypes.POINTER(_sz)
+        L.mo_encode_segments.argtypes = [_pp, _szp, _sz, _u32, _u32, _u8p, _sz, _u32p, _sz,
+                                         _u32p, _u32p]
+        L.mo_encode_segments.restype = _sz
+        L.mo_decode_segments.argtypes = [_u32p, _sz, _u32, _u32, _pp, _szp, _sz, _u32, _u8p,
+                                         ctypes.POINTER(ctypes.c_uint64)]
+        L.mo_decode_segments.restype = ctypes.c_int
         L.mo_multicore_decode.restype = ctypes.c_int
         L.mo_reverse_bytes.argtypes = [_u8p, _sz]
         L.mo_reverse_bytes.restype = None
@@ -178,6 +186,82 @@ def ref_encode(sym: np.ndarray, L: int, seed: int = TABLE_SEED) -> Stream:
         raise ValueError("reference encoding failed")
     return Stream(np.ascontiguousarray(sym, dtype=np.uint8), units[: nu + 4].copy(),
                   int(nu), int(fb[0]), int(fs[0]), dec, L)
+
+
+@dataclass
+class SegStream:
+    """A multi-table stream: one bitstream whose source segments were each
+    encoded with their own table (mo_encode_segments).  Segment lists are in
+    decode order: the source's last segment first."""
+    symbols: np.ndarray      # uint8, source order (all segments)
+    units: np.ndarray        # uint32, n_units + 4 (CUHDInputBuffer order)
+    n_units: int
+    first_bit: int
+    first_state: int
+    L: int
+    tables: list             # uint32 arrays of L decoder words, decode order
+    counts: list             # symbols per segment, decode order
+    starts: list             # bit position of each segment's first codeword, decode order
+
+    @property
+    def n(self) -> int:
+        return int(self.symbols.size)
+
+
+def encode_segments(segs, L: int, seed: int = TABLE_SEED) -> SegStream:
+    """Encodes source segments (uint8 arrays, source order), each with a table
+    built from its own symbols, into one stream; the sequential multi-table
+    decode gives the segments' start positions and must reproduce the
+    source."""
+    encs, decs, mls = [], [], []
+    for sg in segs:
+        enc, dec, ml, _ = build_tables(np.ascontiguousarray(sg, dtype=np.uint8), L, seed)
+        encs.append(enc)
+        decs.append(dec)
+        mls.append(ml)
+    sym = np.concatenate([np.ascontiguousarray(sg, dtype=np.uint8) for sg in segs])
+    ends = np.cumsum([sg.size for sg in segs]).astype(np.uint64)
+    buf = _padded(sym)
+    cap = lib().mo_max_units(max(mls), sym.size) + 4
+    units = np.zeros(cap, dtype=np.uint32)
+    fb = np.zeros(1, dtype=np.uint32)
+    fs = np.zeros(1, dtype=np.uint32)
+    ptrs = (_u32p * len(encs))(*[_ptr(e, _u32p) for e in encs])
+    ends_c = (ctypes.c_size_t * len(segs))(*[int(x) for x in ends])
+    nu = lib().mo_encode_segments(ptrs, ends_c, len(segs), L, max(mls), _ptr(buf, _u8p),
+                                  sym.size, _ptr(units, _u32p), cap, _ptr(fb, _u32p),
+                                  _ptr(fs, _u32p))
+    if nu == 0:
+        raise ValueError("segment encoding failed")
+    tables = decs[::-1]
+    counts = [int(sg.size) for sg in segs][::-1]
+    out = np.zeros(max(1, sym.size), dtype=np.uint8)
+    starts = np.zeros(len(segs), dtype=np.uint64)
+    u = np.ascontiguousarray(units[:nu])
+    dptrs = (_u32p * len(tables))(*[_ptr(t, _u32p) for t in tables])
+    cnt = (ctypes.c_size_t * len(counts))(*counts)
+    rc = lib().mo_decode_segments(_ptr(u, _u32p), int(nu), int(fb[0]), int(fs[0]), dptrs, cnt,
+                                  len(counts), L, _ptr(out, _u8p),
+                                  starts.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    if rc != 0 or not np.array_equal(out[: sym.size][::-1], sym):
+        raise ValueError("segment stream does not decode back to its source")
+    return SegStream(sym, units[: nu + 4].copy(), int(nu), int(fb[0]), int(fs[0]), L,
+                     tables, counts, [int(x) for x in starts])
+
+
+def decode_segments_seq(ss: SegStream) -> np.ndarray:
+    """Sequential multi-table decode: symbols in decode order."""
+    out = np.zeros(max(1, ss.n), dtype=np.uint8)
+    starts = np.zeros(len(ss.counts), dtype=np.uint64)
+    u = np.ascontiguousarray(ss.units[: ss.n_units])
+    dptrs = (_u32p * len(ss.tables))(*[_ptr(t, _u32p) for t in ss.tables])
+    cnt = (ctypes.c_size_t * len(ss.counts))(*ss.counts)
+    rc = lib().mo_decode_segments(_ptr(u, _u32p), ss.n_units, ss.first_bit, ss.first_state,
+                                  dptrs, cnt, len(ss.counts), ss.L, _ptr(out, _u8p),
+                                  starts.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    if rc != 0:
+        raise ValueError("sequential segment decode failed")
+    return out[: ss.n]
 
 
 def make_stream(seed: int, lam: float, n: int, L: int) -> Stream:
