@@ -241,7 +241,8 @@ def profile_figures(workload: str, captured: bool):
 
     traffic = {k: int(v) for k, v in rows("traffic").items()}
     issue = {k: float(v) for k, v in rows("issue").items()}
-    return kernel_of, traffic, issue
+    inst = {k: int(v) for k, v in rows("inst").items()}
+    return kernel_of, traffic, issue, inst
 
 
 def cpu_baseline(st, sample_mb: float):
@@ -489,7 +490,7 @@ def run_ours(args, ws, rank, local):
            "k_prep": st.L * 4, "k_scan": 0}[dom]
     achieved = alg / (mean_k[dom] / 1e3) / 1e9
     wl = f"plain {args.mb:g}MiB lambda={args.lam} L={args.L}"
-    kernel_of, t_rows, issue = profile_figures(wl, captured)
+    kernel_of, t_rows, issue, inst = profile_figures(wl, captured)
     traffic = t_rows.get(kernel_of.get(dom))
     per_sorted = sorted(per_ms)
     cpu = None
@@ -523,7 +524,10 @@ def run_ours(args, ws, rank, local):
                      "frac": round(achieved / hbm, 4), "traffic": traffic,
                      "alg_bytes_per_launch": alg},
         "issue_roofline": {"issue_active_pct": issue, "dominant": kernel_of.get(dom, dom),
-                           "source": "ncu smsp__issue_active (profiles/)"} if issue else None,
+                           "inst_per_symbol": {k: round(v / n, 2) for k, v in inst.items()},
+                           "source": "ncu smsp__issue_active and thread instructions of "
+                                     "one-kernel captures of this workload (profiles/)"}
+        if issue else None,
         "cpu_baseline": cpu,
         "e2e": {"value": round(replica_rate(n, ws, e2e_ms), 3), "unit": "GB/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "bit_exact": e2e_ok,
