@@ -20,6 +20,7 @@ from ._lib import (  # noqa: F401
     DECODE_NO_CAPTURE,
     DECODE_CAPTURE,
     PLAN_MODEL,
+    DECODE_START_OFFSET,
     plan_tuned,
     tune_lookup,
     lib,

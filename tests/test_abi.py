@@ -242,3 +242,62 @@ def test_decode_entry_points_reject_bad_arguments(mg, name, args):
     assert lib.mans_decode(*pos) == mg.Status.ERR_ARG, name
     st = ctypes.c_uint32(0)
     assert lib.mans_decode_sync(*pos, ctypes.byref(st)) == mg.Status.ERR_ARG, name
+
+
+def test_start_offset_flag_widens_first_bit(mg):
+    """MANS_DECODE_START_OFFSET: first_bit is a start offset below 128 bits;
+    without the flag the reference's 0..32 range stands.  Refusals come
+    before any CUDA call (placeholder addresses are never dereferenced)."""
+    import ctypes
+    lib = mg.lib()
+    a = 0x100000
+    v = ctypes.c_void_p
+    st = ctypes.c_uint32(0)
+
+    def call(first_bit, flags):
+        cfg = mg._lib.Cfg(flags=flags)
+        return lib.mans_decode_sync(v(a), 1000, v(a), 5000, v(a), 1024, 1500, first_bit, None,
+                                    1 << 30, ctypes.byref(cfg), None, ctypes.byref(st))
+    # a null workspace fails the checks either way; the first_bit bound is
+    # what differs: 33 and 127 pass it only with the flag, 128 never
+    for fb, flags in ((33, 0), (127, 0), (128, mg.DECODE_START_OFFSET)):
+        assert call(fb, flags) == mg.Status.ERR_ARG, (fb, flags)
+    plan = mg._lib.Cfg(flags=mg.DECODE_START_OFFSET)
+    assert lib.mans_decode(v(a + 4), 1000, v(a), 5000, v(a), 1024, 1500, 100, v(a), 1 << 30,
+                           ctypes.byref(plan), None) == mg.Status.ERR_ARG   # misaligned units
+
+
+def test_trajectory_query_refuses_bad_arguments(mg):
+    import ctypes
+
+    from multians_gb300 import shard
+    be = shard.GpuBackend.__new__(shard.GpuBackend)   # signatures only
+    lib = mg.lib()
+    f = lib.mans_trajectory_query
+    f.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_uint32,
+                  ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_size_t,
+                  ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_uint64),
+                  ctypes.c_uint32, ctypes.POINTER(shard.Point), ctypes.c_void_p,
+                  ctypes.POINTER(ctypes.c_uint32)]
+    f.restype = ctypes.c_int
+    g = lib.mans_trajectory_aux_size
+    g.argtypes = [ctypes.c_size_t, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint32]
+    g.restype = ctypes.c_size_t
+    assert g(1000, 5000, 1024, 0) == 0 and g(1000, 5000, 1024, 1025) == 0
+    need = g(1000, 5000, 1024, 4)
+    assert need > mg.aux_size_max(1000)
+    a = 0x100000
+    q = (ctypes.c_uint64 * 4)(0, 32, 64, 96)
+    out = (shard.Point * 4)()
+    st = ctypes.c_uint32(0)
+    v = ctypes.c_void_p
+    base = [v(a), 1000, v(a), 1024, 1500, 32, 0, 5000, v(a), need, q, 4, out, None,
+            ctypes.byref(st)]
+    cases = {0: v(a + 4), 8: v(None), 9: 100, 11: 0}   # misaligned units, no aux, small aux, nq 0
+    for i, bad in cases.items():
+        args = list(base)
+        args[i] = bad
+        assert f(*args) == mg.Status.ERR_ARG, i
+    args = list(base)
+    args[5] = 33   # first_bit past 32 without the start-offset flag
+    assert f(*args) == mg.Status.ERR_ARG
