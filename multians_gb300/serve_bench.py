@@ -287,7 +287,7 @@ def measure(args, ws, rank, local):
         "cpu_baseline": None,
         "e2e": {"value": round(ws * total_sym / e2e_s / 1e9, 3), "unit": "GB/s",
                 "h2d_bytes_per_step": total_comp, "d2h_bytes_per_step": total_sym},
-        "gpu_launches": int(round(4 * batches)),
+        "gpu_launches": int(round((s1["kernel_launches"] - s0["kernel_launches"]) / steps)),
         "server": {"batches_per_step": round(batches, 1), "largest_batch": stats["largest_batch"],
                    "admission_waits": stats["admission_waits"], "range_peak": stats["range_peak"],
                    "streams_redone": stats["streams_redone"], "failed": stats["failed"]},
