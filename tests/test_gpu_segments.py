@@ -67,3 +67,20 @@ def test_single_symbol_table_before_the_last_segment_is_refused(mg, oracle_lib):
     with pytest.raises(mg.MansError):
         segments.decode_segments(_dev(ss.units), ss.n_units, ss.first_state, ss.first_bit,
                                  1024, tables, ss.counts, ss.starts)
+
+
+def test_one_segment_is_a_plain_stream(mg, oracle_lib):
+    """A single segment is an ordinary stream: the segment decoder gives the
+    plain decoder's output."""
+    import torch
+    from multians_gb300 import segments
+    O = oracle_lib
+    sym = O.gen_symbols(31, 0.05, 200_000)
+    st = O.encode(sym, 1024)
+    got, info = segments.decode_segments(_dev(st.units), st.n_units, st.first_state,
+                                         st.first_bit, 1024, [st.table], [st.n],
+                                         [32 - st.first_bit])
+    plain = mg.decode(_dev(st.units), st.n_units, st.n, _dev(st.table), st.first_state,
+                      st.first_bit, L=1024)
+    assert torch.equal(got, plain)
+    assert np.array_equal(got.cpu().numpy()[::-1], sym)

@@ -1,5 +1,5 @@
 """One stream split over several ranks (multians_gb300/shard.py), on the CPU:
-world-size 2 and 3 gloo process groups run the exchange protocol with a
+world-size 2, 3 and 4 gloo process groups run the exchange protocol with a
 sequential slice decoder (the reference's per-symbol step,
 src/multians_gpu_decoder.cu:131-167, restated here as test infrastructure)
 in place of the GPU, and the concatenated outputs must equal the oracle's
@@ -81,7 +81,7 @@ def _worker(rank, ws, port, outdir, stream_file, prefix_units):
 
 
 @pytest.mark.parametrize("ws,lam,L,prefix", [(2, 0.05, 1024, None), (3, 1.0, 1024, None),
-                                             (2, 0.2, 4096, 2)])
+                                             (2, 0.2, 4096, 2), (4, 2.0, 1024, 3)])
 def test_sharded_decode_matches_the_oracle(tmp_path, oracle_lib, ws, lam, L, prefix):
     torch = pytest.importorskip("torch")
     import torch.multiprocessing as mp
