@@ -43,7 +43,6 @@ and value sums the ranks' decoded bytes over the slowest rank's time.
 from __future__ import annotations
 
 import argparse
-import ctypes
 import json
 import os
 import statistics

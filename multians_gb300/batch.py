@@ -5,7 +5,7 @@ from __future__ import annotations
 
 import ctypes
 
-from ._lib import Cfg, MansError, check, lib
+from ._lib import Cfg, check, lib
 
 
 class StreamDesc(ctypes.Structure):
