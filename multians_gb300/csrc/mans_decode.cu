@@ -252,6 +252,32 @@ __device__ __forceinline__ uint32_t cap_row(uint32_t col, uint32_t c) {
     return col + ((c << 5) & 0xF80u);   // row (c / 4) mod 32
 }
 
+// Decodes trajectory A with capture until its cursor reaches relative bit
+// `be`; cs is 32 x its count (bits 7..11: the ring row).  kAligned: the
+// capture rows start on a 4 KB boundary, so a row address is the column OR
+// the offset (one logic operation).
+template <bool kAligned>
+__device__ __forceinline__ uint32_t cap_run(SCursor& A, const UnitSrc& src, CapLane& cl,
+                                            uint32_t cs, uint32_t be) {
+    while (A.pos < be) {
+        cl.acc = __byte_perm(cl.acc, A.step(src), 0x7321);
+        sts32(kAligned ? (cl.col | (cs & 0xF80u)) : cl.col + (cs & 0xF80u), cl.acc);
+        cs += 32;
+    }
+    return cs;
+}
+
+// Largest code length k of the shared table's L entries (all threads of
+// the CTA; a barrier per bit).
+__device__ __forceinline__ uint32_t table_kmax(const uint2* s_tab, uint32_t L) {
+    uint32_t km = 0;
+    for (uint32_t j = threadIdx.x; j < L; j += blockDim.x) km = max(km, (s_tab[j].y >> 16) & 0xffu);
+    uint32_t kmax = 0;
+    for (uint32_t bit = 16; bit; bit >>= 1)
+        if (__syncthreads_or(km >= kmax + bit)) kmax += bit;
+    return kmax;
+}
+
 // Copies the completed groups of the first `count` symbols (all of them,
 // the last group padded, when `final`) to dst, at most `limit` bytes
 // (a multiple of 16).
@@ -296,6 +322,9 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
     extern __shared__ __align__(16) uint2 s_tab[];
     // capture decodes symbol by symbol; otherwise zero-bit runs are folded
     load_prepared(s_tab, kCap ? p.tab_sym : p.tab_sync, p.L);
+    // the uncaptured pass steps four at a time while the fourth step surely
+    // starts before the half-block end (a step moves at most kmax bits)
+    const uint32_t kgrp = kCap ? 0u : 3 * table_kmax(s_tab, p.L);
     if (*(volatile uint32_t*) p.status & (MANS_DEV_BAD_TABLE | MANS_DEV_DEGENERATE)) return;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t tb = smem_addr(s_tab);
@@ -418,14 +447,15 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
             // decode to the end of the half block
             const uint32_t be = bs + Hbits;
             if (kCap) {
-                uint32_t cs = ca << 5;   // 32 x count: its bits 7..11 pick the ring row
-                while (A.pos < be) {
-                    cl.acc = __byte_perm(cl.acc, A.step(rs), 0x7321);
-                    sts32(cl.col | (cs & 0xF80u), cl.acc);
-                    cs += 32;
-                }
-                ca = cs >> 5;
+                ca = cap_run<true>(A, rs, cl, ca << 5, be) >> 5;
             } else {
+                // measured at 256 MiB: 0.319 -> 0.314 ms (6 bits per symbol), L = 4096
+                // at 1.5 bits per symbol 1.91 -> 1.82 ms
+                while (A.pos + kgrp < be) {
+                    const uint32_t y0 = A.step(rs), y1 = A.step(rs);
+                    const uint32_t y2 = A.step(rs), y3 = A.step(rs);
+                    ca += (y0 >> 24) + (y1 >> 24) + (y2 >> 24) + (y3 >> 24);
+                }
                 while (A.pos < be) ca += A.step(rs) >> 24;
             }
             bs = be;
@@ -706,20 +736,9 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
                 }
                 if (sa && cl.on) {
                     // d == 1: capture, flushing at the half block and the block end
-                    uint32_t cs = ca << 5;
-                    const uint32_t mid = bs + (Bbits >> 1);
-                    while (A.pos < mid) {
-                        cl.acc = __byte_perm(cl.acc, A.step(src), 0x7321);
-                        sts32(cl.col + (cs & 0xF80u), cl.acc);
-                        cs += 32;
-                    }
+                    uint32_t cs = cap_run<false>(A, src, cl, ca << 5, bs + (Bbits >> 1));
                     cap_flush(cl, slice, cs >> 5, p.cap_bytes, false);
-                    while (A.pos < be) {
-                        cl.acc = __byte_perm(cl.acc, A.step(src), 0x7321);
-                        sts32(cl.col + (cs & 0xF80u), cl.acc);
-                        cs += 32;
-                    }
-                    ca = cs >> 5;
+                    ca = cap_run<false>(A, src, cl, cs, be) >> 5;
                     cap_flush(cl, slice, ca, p.cap_bytes, false);
                     if (!cl.on) p.cap_valid[jk] = cl.done;   // the capture broke off
                 }
@@ -1296,8 +1315,69 @@ __device__ __forceinline__ void out_copy(uint8_t* __restrict__ out, unsigned lon
     }
 }
 
+// Staging bytes per warp of k_copy: a segment whose aligned source range
+// (plus a word of read slack) fits is copied through shared memory.
+constexpr uint32_t kCopyStage = 4096;
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// out_copy through the warp's staging buffer: the segment's 16-byte aligned
+// source chunks are copied in with cp.async (all of them in flight at once,
+// one DRAM round trip), then every lane assembles its 16-byte output chunks
+// from five shared words, as out_copy does from global ones.
 template <bool kRev>
-__device__ __forceinline__ void copy_body(const DecodeParams& p, uint32_t cta, uint32_t nctas) {
+__device__ __forceinline__ void out_copy_staged(uint8_t* __restrict__ out, unsigned long long n_out,
+                                                unsigned long long o0, unsigned long long o1,
+                                                const uint8_t* __restrict__ cap,
+                                                unsigned long long src0, uint32_t lane,
+                                                uint32_t stage) {
+    const uint32_t len = (uint32_t) (o1 - o0);
+    const unsigned long long s_lo = src0 & ~15ull;
+    const uint32_t sh0 = (uint32_t) (src0 - s_lo);
+    const uint32_t nsrc = (sh0 + len + 15) >> 4;
+    for (uint32_t c = lane; c < nsrc; c += 32) cp_async16(stage + c * 16, cap + s_lo + c * 16);
+    cp_async_wait_all();
+    __syncwarp();
+    const unsigned long long y0 = kRev ? n_out - o1 : o0;
+    const uint32_t head = min(len, (uint32_t) ((16u - (((uintptr_t) out + y0) & 15u)) & 15u));
+    const uint32_t nc = (len - head) >> 4;
+    const uint32_t tail = (len - head) & 15u;
+    if (lane < head + tail) {
+        const uint32_t j = lane < head ? lane : head + nc * 16 + (lane - head);
+        const uint32_t e = kRev ? sh0 + len - 1 - j : sh0 + j;
+        out[y0 + j] = (uint8_t) (lds32(stage + (e & ~3u)) >> (8u * (e & 3u)));
+    }
+    for (uint32_t c = lane; c < nc; c += 32) {
+        const uint32_t j = head + 16 * c;
+        const uint32_t e = kRev ? sh0 + len - 16 - j : sh0 + j;
+        const uint32_t q = stage + (e & ~3u), sh = (e & 3u) * 8u;
+        const uint32_t w0 = lds32(q), w1 = lds32(q + 4), w2 = lds32(q + 8), w3 = lds32(q + 12),
+                       w4 = lds32(q + 16);
+        uint4 v;
+        if (!kRev) {
+            v.x = __funnelshift_r(w0, w1, sh);
+            v.y = __funnelshift_r(w1, w2, sh);
+            v.z = __funnelshift_r(w2, w3, sh);
+            v.w = __funnelshift_r(w3, w4, sh);
+        } else {
+            v.x = __byte_perm(__funnelshift_r(w3, w4, sh), 0, 0x0123);
+            v.y = __byte_perm(__funnelshift_r(w2, w3, sh), 0, 0x0123);
+            v.z = __byte_perm(__funnelshift_r(w1, w2, sh), 0, 0x0123);
+            v.w = __byte_perm(__funnelshift_r(w0, w1, sh), 0, 0x0123);
+        }
+        __stcs(reinterpret_cast<uint4*>(out + y0 + j), v);
+    }
+    __syncwarp();   // the buffer is refilled by the next segment
+}
+
+template <bool kRev>
+__device__ __forceinline__ void copy_body(const DecodeParams& p, uint32_t cta, uint32_t nctas,
+                                          uint32_t stage_base) {
     const uint32_t st = *(volatile uint32_t*) p.status;
     if (st & MANS_DEV_DEGENERATE) {
         const uint8_t sym = (uint8_t) (__ldg(p.table) >> 16);
@@ -1350,13 +1430,20 @@ __device__ __forceinline__ void copy_body(const DecodeParams& p, uint32_t cta, u
         const unsigned long long src0 = __shfl_sync(0xffffffffu, e.src, s0);
         const unsigned long long o0 = __shfl_sync(0xffffffffu, e.off, s0);
         const unsigned long long o1 = __shfl_sync(0xffffffffu, o_end, last);
+        // measured at 256 MiB, 6 bits per symbol: copy pass 0.138 -> 0.130 ms
+        if ((src0 & 15ull) + (o1 - o0) + 32 <= kCopyStage) {
+            out_copy_staged<kRev>(p.out, p.n_out, o0, o1, p.cap, src0, lane,
+                                  stage_base + (threadIdx.x >> 5) * kCopyStage);
+            continue;
+        }
         out_copy<kRev>(p.out, p.n_out, o0, o1, p.cap, src0, lane);
     }
 }
 
 template <bool kRev>
 __global__ void __launch_bounds__(kCopyThreads) k_copy(DecodeParams p) {
-    copy_body<kRev>(p, blockIdx.x, gridDim.x);
+    __shared__ __align__(16) uint8_t s_stage[(kCopyThreads / 32) * kCopyStage];
+    copy_body<kRev>(p, blockIdx.x, gridDim.x, smem_addr(s_stage));
 }
 
 // The decoding final pass over the warps k_copy listed (persistent grid).
@@ -1518,8 +1605,10 @@ __global__ void __launch_bounds__(kCopyThreads) k_copy_batch(const DecodeParams*
     const BatchItem it = items[blockIdx.x];
     load_params(sp, ps + it.stream);
     if (!sp.cap_bytes) return;
-    if (sp.flags & MANS_DECODE_SOURCE_ORDER) copy_body<true>(sp, it.index, it.count);
-    else copy_body<false>(sp, it.index, it.count);
+    __shared__ __align__(16) uint8_t s_stage[(kCopyThreads / 32) * kCopyStage];
+    const uint32_t stage = smem_addr(s_stage);
+    if (sp.flags & MANS_DECODE_SOURCE_ORDER) copy_body<true>(sp, it.index, it.count, stage);
+    else copy_body<false>(sp, it.index, it.count, stage);
 }
 
 __global__ void __launch_bounds__(kFinalThreads) k_final_batch(const DecodeParams* ps,
