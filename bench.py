@@ -81,6 +81,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-capture", action="store_true",
                     help="decode without symbol capture (MANS_DECODE_NO_CAPTURE)")
+    ap.add_argument("--seeds", choices=["auto", "on", "off"], default="auto",
+                    help="seeded merge walks: the planner's choice, or forced "
+                         "(MANS_DECODE_SEEDS / MANS_DECODE_NO_SEEDS)")
     ap.add_argument("--cpu-sample-mb", type=float, default=32.0)
     ap.add_argument("--no-subrecords", action="store_true",
                     help="plain workload: leave out the batched and served sub-records")
@@ -339,7 +342,9 @@ def run_ours(args, ws, rank, local):
     table = table_h.to(dev)
     out = torch.empty(n, dtype=torch.uint8, device=dev)
     out_h = torch.empty(n, dtype=torch.uint8).pin_memory()
-    cfg = mg.plan(st.n_units, n, st.L, {"flags": mg.DECODE_NO_CAPTURE} if args.no_capture else None)
+    hint_flags = (mg.DECODE_NO_CAPTURE if args.no_capture else 0) | \
+        {"auto": 0, "on": mg.DECODE_SEEDS, "off": mg.DECODE_NO_SEEDS}[args.seeds]
+    cfg = mg.plan(st.n_units, n, st.L, {"flags": hint_flags} if hint_flags else None)
     aux = torch.empty(mg.aux_size(st.n_units, cfg), dtype=torch.uint8, device=dev)
     want = torch.from_numpy(np.ascontiguousarray(st.symbols[::-1])).to(dev)
     stream = torch.cuda.current_stream(dev)

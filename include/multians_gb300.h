@@ -98,6 +98,18 @@ typedef struct {
  * and mans_trajectory_query. */
 #define MANS_DECODE_START_OFFSET 0x10u
 
+/* Seeded merge walks.  The walk pass lasts as long as its longest merge
+ * walk, one dependent chain of table lookups.  With seeds, a warp whose
+ * last walk is still running after two of its windows puts its idle lanes
+ * to decoding from guessed states at the blocks ahead of that walk; where
+ * the walk's trajectory meets one of theirs it continues from that lane's
+ * position.  The planner turns seeds on where that was measured to pay
+ * (1 to 4.5 bits per symbol; to 7 at L >= 4096); MANS_DECODE_SEEDS turns them on and
+ * MANS_DECODE_NO_SEEDS off whatever the stream.  The output is identical
+ * either way.  Plain decodes only (batches walk without seeds). */
+#define MANS_DECODE_SEEDS 0x20u
+#define MANS_DECODE_NO_SEEDS 0x40u
+
 /* Fills `out` with the geometry the decoder uses for this call: the built-in
  * autotuner, keyed on the table size L and the compression ratio (bits per
  * symbol = 32 n_units / n_out).  Where the hint fixes no geometry and no
@@ -192,7 +204,7 @@ typedef struct {
     uint32_t unmerged;         /* walks that reached the stream end without merging
                                   (or ran out of walk slots: MANS_DEV_SYNC_OVERFLOW,
                                   counted to the stream end) */
-    uint32_t reserved;
+    uint32_t seeded_walks;     /* walks finished with seeds (MANS_DECODE_SEEDS) */
 } mans_sync_stats;
 
 int mans_sync_stats_get(const void* d_aux, size_t aux_bytes, size_t n_units, size_t n_out,

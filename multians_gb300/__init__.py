@@ -21,6 +21,8 @@ from ._lib import (  # noqa: F401
     DECODE_CAPTURE,
     PLAN_MODEL,
     DECODE_START_OFFSET,
+    DECODE_SEEDS,
+    DECODE_NO_SEEDS,
     plan_tuned,
     tune_lookup,
     lib,

@@ -41,6 +41,8 @@ DECODE_SOURCE_ORDER = 0x1
 DECODE_NO_CAPTURE = 0x2
 DECODE_CAPTURE = 0x4
 DECODE_START_OFFSET = 0x10
+DECODE_SEEDS = 0x20
+DECODE_NO_SEEDS = 0x40
 PLAN_MODEL = 0x8
 
 
@@ -59,7 +61,7 @@ class SyncStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "regions", "blocks", "walks", "open_walks", "walk_units", "walk_max_units",
         "walk_blocks", "metadata_bytes", "fallback_warps")] + [
-        ("unmerged", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+        ("unmerged", ctypes.c_uint32), ("seeded_walks", ctypes.c_uint32)]
 
 
 class Cfg(ctypes.Structure):
@@ -194,7 +196,7 @@ def sync_stats(d_aux: int, aux_bytes: int, n_units: int, n_out: int, L: int,
     check(lib().mans_sync_stats_get(d_aux, aux_bytes, n_units, n_out, L,
                                     ctypes.byref(c) if c is not None else None, stream,
                                     ctypes.byref(out)), "mans_sync_stats_get")
-    return {f: int(getattr(out, f)) for f, _ in SyncStats._fields_ if f != "reserved"}
+    return {f: int(getattr(out, f)) for f, _ in SyncStats._fields_}
 
 
 KERNELS = ("k_prep", "k_gwalk", "k_wwalk", "k_scan", "k_final")

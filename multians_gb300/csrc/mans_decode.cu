@@ -94,6 +94,7 @@ struct DecodeParams {
     uint32_t* cap_valid;   // [nreg] leading symbols of Gamma_k captured in slice k
     uint32_t cap_bytes;    // capture bytes per region (0: no capture)
     uint32_t* fb_list;     // [nblk / 32] warps the copy pass leaves to the decoding pass
+    uint2* seed_ring;      // [kSeedSlots * 32 * kSeedRing] seeded-walk records (null: no seeds)
 };
 
 // Checks and converts the reference table, then builds both shared-memory
@@ -188,6 +189,23 @@ struct WJob {          // stored as two uint4
     uint32_t pad;
 };
 static_assert(sizeof(WJob) == 32, "job record layout");
+
+// A merge walk still running: the G pass marks every walk it hands over,
+// the walk pass publishes the result (delta first, then m, after a fence).
+constexpr unsigned long long kMergePending = ~1ull;
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* a) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(a) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void publish_merge(const DecodeParams& p, uint32_t k,
+                                              unsigned long long m, long long delta) {
+    p.delta[k] = delta;
+    if (p.seed_ring) __threadfence();   // only seeded walks read other walks' results
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p.m + k), "l"(m) : "memory");
+}
 
 // Sync stage, G pass (k_gwalk): every lane owns a ring of kRingSlots chunks
 // of kChunk units in shared memory, filled by TMA bulk copies.  The warp
@@ -434,6 +452,7 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
                 p.delta[k] = (long long) ca - (long long) rg.y;
                 active = false;
             } else if (b == wend) {
+                p.m[k] = kMergePending;
                 const uint32_t slot = atomicAdd(p.scan_flags + ntile + 1, 1u);
                 uint4* dst = reinterpret_cast<uint4*>(p.walk_jobs + slot);
                 dst[0] = make_uint4(k, b, ax, ca);
@@ -487,6 +506,7 @@ __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase
                         wend = b1 + p.wcap;
                         rg = __ldcg(p.rec_g + b1);
                     } else {
+                        p.m[k] = kMergePending;
                         const uint32_t slot = atomicAdd(p.scan_flags + ntile + 1, 1u);
                         uint4* dst = reinterpret_cast<uint4*>(p.walk_jobs + slot);
                         dst[0] = make_uint4(k, b1, rec.x, rec.y);
@@ -553,7 +573,294 @@ constexpr uint32_t kWindowUnits = 128;
 constexpr uint32_t kWindowTile = (kWindowUnits + 4) * 4;     // bytes per lane
 constexpr uint32_t kWindowStride = kWindowTile;   // 132 words: 8 bank groups, 16-byte aligned
 
+// Seeded walks (the tail of the walk pass).  The walk pass lasts as long
+// as its longest walk, a dependent chain of table lookups.  When a warp has
+// one walk left and the job list is empty, its 31 idle lanes become seeds:
+// trajectories decoded from a guessed state (the stream's first state, bit
+// 0 of the block) at the blocks just ahead of the walker, each recording its
+// entry and count at every block start in a ring.  Decodes that stand at the
+// same bit in the same state are identical from there on, so when the
+// walker's entry at block b equals a seed's record at b, the walker's
+// trajectory is that seed's from b: the seed writes its records for the
+// blocks after b as the walk's (counts shifted by the difference at b) and
+// carries the walk on, from where it stands.  The farthest matching seed is
+// taken; idle lanes are seeded again ahead of the others at window ends.
+//
+// The walk ends where its trajectory meets Gamma_{k+1}'s at a block start.
+// Every lane looks Gamma_{k+1} up in memory: its G-pass records inside region
+// k + 1, and past that the records of the walks that continue it (walk k + 1
+// up to its merge, then Gamma_{k+2}, and so on, counts shifted by the deltas).
+// A seed that meets Gamma_{k+1} stops there; a walker that takes such a seed
+// ends the walk at the seed's stop.  A merge found later than the first one
+// is still a block start where both trajectories agree (they stay equal), so
+// m and delta are valid either way.
+constexpr uint32_t kSeedSlots = 32;    // warps that may seed at once
+constexpr uint32_t kSeedRing = 32;     // blocks of records a seed keeps
+constexpr uint32_t kSeedMinWindows = 2;   // windows a walk runs in the walk pass first
+constexpr uint32_t kBmUnknown = 0xfffffffeu;
+
+// Where Gamma_{k+1} stands at block starts, read from memory.
+struct NextLookup {
+    uint32_t j;       // Gamma_{k+1} runs on Gamma_j here (with a count offset)
+    uint32_t bm;      // block of walk j's merge (~0: none; kBmUnknown: not read yet)
+    long long off;    // Gamma_{k+1}'s count - Gamma_j's count
+};
+
+// Gamma_{k+1}'s entry and count at block b (blocks asked in increasing order).
+// 0: found; 1: a walk it depends on is still running; 2: not available.
+__device__ __forceinline__ int next_lookup(const DecodeParams& p, NextLookup& L, uint32_t b,
+                                           uint32_t& x, uint32_t& c) {
+    const uint32_t r = b / p.nb;
+    for (uint32_t it = 0; it < kMaxWalkSlots + 2; ++it) {
+        if (r < L.j) return 2;
+        if (r == L.j) {
+            const uint2 e = __ldcg(p.rec_g + b);
+            x = e.x;
+            c = (uint32_t) ((long long) e.y + L.off);
+            return 0;
+        }
+        if (L.bm == kBmUnknown) {
+            const unsigned long long mj = ld_acquire_u64(p.m + L.j);
+            if (mj == kMergePending) return 1;
+            L.bm = mj == ~0ull ? ~0u : (uint32_t) (mj / (p.B * 32));
+        }
+        if (b <= L.bm) {
+            const uint32_t d = r - L.j;
+            if (d > p.dmax) return 2;
+            const uint2 e = __ldcg(p.rec_w + (size_t) b * p.dmax + (d - 1));
+            x = e.x;
+            c = (uint32_t) ((long long) e.y + L.off);
+            return 0;
+        }
+        L.off += __ldcg(p.delta + L.j);
+        ++L.j;
+        L.bm = kBmUnknown;
+    }
+    return 2;
+}
+
+// Stages units [u0, u0 + tile_units) of the lanes with `on` into their
+// tiles and waits for the copies (phase `win` of the warp's barrier).
+__device__ __forceinline__ void stage_window(const DecodeParams& p, bool on, uint32_t u0,
+                                             uint32_t tile, uint32_t tile_units, uint32_t bar,
+                                             uint32_t win, bool& timed_out) {
+    const uint32_t n = p.n_units;
+    const uint32_t avail = (on && u0 < n) ? min(tile_units, n - u0) : 0u;
+    const uint32_t bulk = avail & ~3u;
+    const uint32_t total = __reduce_add_sync(0xffffffffu, bulk * 4);
+    if ((threadIdx.x & 31) == 0) mbar_arrive_expect_tx(bar, total);
+    __syncwarp();
+    if (bulk) {
+        fence_proxy_async();
+        tma_load(tile, p.units + u0, bulk * 4, bar);
+    }
+    if (on)
+        for (uint32_t i = bulk; i < tile_units; ++i)
+            sts32(tile + i * 4, i < avail ? __ldg(p.units + u0 + i) : 0u);
+    if (!mbar_wait(bar, win & 1)) {
+        timed_out = true;
+        mbar_wait(bar, win & 1);
+    }
+    __syncwarp();
+}
+
+
+// Runs walk k (the walker lane wl stands at block jb with entry arec and
+// count cnt) to its end with the warp's other lanes as seeds; ring: the
+// lane's part of the warp's slot of seed records.  All lanes call it.  The
+// memory every block start needs (Gamma_{k+1}'s entry there, and a seed's
+// record at the walker's next block) is loaded one block ahead, while the
+// lane decodes its current block.
+// A call, not inlined: inlined it pushed the uncaptured walk loop into
+// spills.
 template <bool kCap>
+__device__ __noinline__ void seeded_walk(const DecodeParams& p, uint32_t tb, uint32_t tile, uint32_t bar,
+                            uint32_t& win, bool& timed_out, uint32_t wl, uint32_t k,
+                            uint32_t jb, uint32_t arec, uint32_t cnt, uint2* __restrict__ ring) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t B = p.B, Bbits = p.B * 32, nwb = kWindowUnits / p.B;
+    const uint32_t tile_units = kWindowUnits + 4;
+    const uint32_t kgrp = kCap ? 0u : 3 * 16u;   // a step moves at most 16 bits
+    // lane roles: 0 idle, 1 walker, 2 seed
+    uint32_t role = lane == wl ? 1u : 0u;
+    uint32_t pb = jb, st = jb;
+    bool stopped = false;
+    uint32_t sgc = 0;    // a stopped seed: Gamma_{k+1}'s count at its stop
+    NextLookup L{k + 1, kBmUnknown, 0};
+    // Gamma_{k+1} at this lane's block pb, looked up ahead (nrc: 0 found,
+    // 1 pending, 2 unavailable, 3 not looked up yet)
+    uint32_t ngx = 0, ngc = 0;
+    int nrc = 3;
+    // the record at the walker's block, loaded ahead (for block rwb)
+    uint2 rw = make_uint2(0, 0);
+    uint32_t rwb = ~0u;
+    uint32_t cur_wl = wl;
+    bool done = false;   // the walk has ended (warp-uniform)
+    const uint32_t max_iter = (p.dmax + 2) * p.nb + 2 * kSeedRing;
+    uint32_t iter = 0;
+    for (;;) {
+        // seed the idle lanes ahead of every active lane, within reach of the
+        // walker's comparisons (kSeedRing blocks)
+        {
+            const uint32_t pbw = __shfl_sync(0xffffffffu, pb, cur_wl);
+            const uint32_t front = __reduce_max_sync(0xffffffffu, role ? pb : 0u);
+            const uint32_t idle = __ballot_sync(0xffffffffu, role == 0);
+            if (role == 0) {
+                const uint32_t rank = __popc(idle & ((1u << lane) - 1));
+                const uint32_t nb0 = front + 1 + rank;
+                if (nb0 < p.nblk && nb0 < pbw + kSeedRing &&
+                    nb0 / p.nb <= k + p.dmax) {
+                    role = 2;
+                    st = pb = nb0;
+                    arec = p.first_idx << 8;
+                    cnt = 0;
+                    stopped = false;
+                    L = NextLookup{k + 1, kBmUnknown, 0};
+                    nrc = 3;
+                    rwb = ~0u;
+                }
+            }
+        }
+        const bool mov = role != 0 && !stopped;
+        const uint32_t u0 = pb * B;
+        stage_window(p, mov, u0, tile, tile_units, bar, win, timed_out);
+        ++win;
+        const UnitSrc src{tile, u0, ~0u, tile_units - 1};
+        const uint64_t origin = (uint64_t) u0 * 32;
+        SCursor A;
+        if (mov) A.init(src, origin, origin + (arec & 0xffu), tb + 8u * min(arec >> 8, p.L - 1));
+        uint32_t bs = 0;
+        const bool moved = mov;   // this lane's cursor stands in this window's tile
+        for (uint32_t i = 0; i < nwb; ++i, bs += Bbits) {
+            bool fin = false;
+            unsigned long long fm = 0;
+            long long fd = 0;
+            uint32_t ex = 0;
+            const bool act = role != 0 && !stopped && moved;
+            if (act) {
+                ex = (A.pos - bs) | (entry_index(A.a, tb) << 8);
+                const uint32_t d = pb / p.nb - k;
+                if (pb >= p.nblk || d > p.dmax || d == 0) {
+                    if (role == 1) {
+                        if (pb < p.nblk) atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
+                        fin = true;
+                        fm = ~0ull;
+                    }
+                    role = 0;
+                } else {
+                    uint32_t gx = ngx, gc = ngc;
+                    int rc = nrc;
+                    if (rc == 3) rc = next_lookup(p, L, pb, gx, gc);
+                    if (role == 1) {
+                        // the walker waits (bounded) for the walk it needs
+                        for (uint32_t w = 0; rc == 1 && w < (1u << 20); ++w) {
+                            __nanosleep(256);
+                            rc = next_lookup(p, L, pb, gx, gc);
+                        }
+                        p.rec_w[(size_t) pb * p.dmax + (d - 1)] = make_uint2(ex, cnt);
+                        if (rc != 0) {
+                            atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
+                            fin = true;
+                            fm = ~0ull;
+                        } else if (ex == gx) {
+                            fin = true;
+                            fm = (uint64_t) pb * Bbits + (ex & 0xffu);
+                            fd = (long long) cnt - (long long) gc;
+                        }
+                    } else {
+                        ring[pb % kSeedRing] = make_uint2(ex, cnt);
+                        if (rc == 0 && ex == gx) {   // a running walk: not checked here
+                            stopped = true;
+                            sgc = gc;
+                        }
+                    }
+                }
+            }
+            // the walker's entry against the seeds' records at its block
+            const uint32_t pbw = __shfl_sync(0xffffffffu, pb, cur_wl);
+            const uint32_t exw = __shfl_sync(0xffffffffu, ex, cur_wl);
+            const uint32_t cw = __shfl_sync(0xffffffffu, cnt, cur_wl);
+            const bool wact = __shfl_sync(0xffffffffu, (int) act, cur_wl) != 0;
+            const bool anyfin = __any_sync(0xffffffffu, fin);
+            uint32_t key = 0;
+            if (wact && !anyfin && role == 2 && (moved || stopped) && st <= pbw && pbw < pb &&
+                pb - pbw < kSeedRing) {
+                if (rwb != pbw) rw = ring[pbw % kSeedRing];
+                if (rw.x == exw) key = pb + 1;
+            }
+            const uint32_t kmx = __reduce_max_sync(0xffffffffu, key);
+            if (kmx) {
+                const uint32_t ns = __ffs(__ballot_sync(0xffffffffu, key == kmx)) - 1;
+                if (lane == ns) {
+                    // the walk runs on this seed's trajectory from pbw on
+                    const long long off = (long long) cw - (long long) rw.y;
+                    for (uint32_t b = pbw + 1; b <= pb; ++b) {
+                        const uint2 r = ring[b % kSeedRing];
+                        p.rec_w[(size_t) b * p.dmax + (b / p.nb - k - 1)] =
+                            make_uint2(r.x, (uint32_t) ((long long) r.y + off));
+                    }
+                    cnt = (uint32_t) ((long long) cnt + off);
+                    if (stopped) {
+                        fin = true;
+                        fm = (uint64_t) pb * Bbits + (ring[pb % kSeedRing].x & 0xffu);
+                        fd = (long long) cnt - (long long) sgc;
+                        role = 0;
+                    } else {
+                        role = 1;
+                    }
+                } else if (lane == cur_wl || (role == 2 && pb <= kmx - 1)) {
+                    role = 0;   // behind the new walker
+                }
+                cur_wl = ns;
+            }
+            if (__any_sync(0xffffffffu, fin)) {
+                if (fin) publish_merge(p, k, fm, fd);
+                done = true;
+                break;
+            }
+            // look ahead: Gamma_{k+1} at this lane's next block, and the
+            // record at the walker's next block
+            const bool step = role != 0 && !stopped && moved;
+            nrc = 3;
+            if (step && pb + 1 < p.nblk) nrc = next_lookup(p, L, pb + 1, ngx, ngc);
+            const uint32_t pbn = __shfl_sync(0xffffffffu, pb, cur_wl) + 1;
+            rwb = ~0u;
+            if (role == 2 && st <= pbn && pbn <= pb && pb - pbn < kSeedRing) {
+                rw = ring[pbn % kSeedRing];
+                rwb = pbn;
+            }
+            // every moving lane walks its block
+            if (step) {
+                const uint32_t be = bs + Bbits;
+                if (kCap) {
+                    while (A.pos < be) { A.step(src); ++cnt; }
+                } else {
+                    while (A.pos + kgrp < be) {
+                        const uint32_t y0 = A.step(src), y1 = A.step(src);
+                        const uint32_t y2 = A.step(src), y3 = A.step(src);
+                        cnt += (y0 >> 24) + (y1 >> 24) + (y2 >> 24) + (y3 >> 24);
+                    }
+                    while (A.pos < be) cnt += A.step(src) >> 24;
+                }
+                ++pb;
+            }
+        }
+        if (done) break;
+        if (role != 0 && !stopped && moved) arec = (A.pos - bs) | (entry_index(A.a, tb) << 8);
+        // a stopped seed behind the walker is of no more use
+        const uint32_t pbw = __shfl_sync(0xffffffffu, pb, cur_wl);
+        if (role == 2 && stopped && pb < pbw) role = 0;
+        if (++iter > max_iter) {   // cannot happen for a walk within its slots
+            if (lane == cur_wl) {
+                atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
+                publish_merge(p, k, ~0ull, 0);
+            }
+            break;
+        }
+    }
+}
+
+template <bool kCap, bool kSeeds>
 __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
     extern __shared__ __align__(16) uint2 s_tab[];
     const uint32_t ntile = (p.nreg + kScanTile - 1) / kScanTile;
@@ -594,6 +901,7 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
     // job: region jk, block jb; A: entry a_rec, count ca (offset to Gamma_j's
     // count while following); G likewise (g_rec = ~0: not a cursor yet)
     uint32_t jk = 0, jb = 0, a_rec = 0, ca = 0, g_rec = ~0u, cg = 0, fl = 0;
+    uint32_t wins = 0;   // windows walked on the current job
     bool timed_out = false;
     CapLane cl;
     cl.col = ((tb + tab_bytes + blockDim.x * kWindowStride + (blockDim.x >> 5) * 8 + 15) & ~15u) +
@@ -618,6 +926,7 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
                     jk = v0.x; jb = v0.y; a_rec = v0.z; ca = v0.w;
                     g_rec = v1.x; cg = v1.y; fl = v1.z;
                     open = true;
+                    wins = 0;
                     if (kCap) {
                         // capture goes on where the G pass's was complete
                         slice = p.cap + (size_t) jk * p.cap_bytes;
@@ -641,6 +950,51 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
             }
         }
         if (!__any_sync(0xffffffffu, open)) break;
+        if (kSeeds && p.seed_ring && exhausted) {
+            // one long walk left in this warp and no jobs: seed it
+            const uint32_t om = __ballot_sync(0xffffffffu, open);
+            const uint32_t wl = __ffs(om) - 1;
+            if (__popc(om) == 1 && __shfl_sync(0xffffffffu, wins, wl) >= kSeedMinWindows) {
+                uint32_t* const mask = p.scan_flags + ntile + 4;
+                uint32_t slot = ~0u;
+                if (lane == 0)
+                    for (int t = 0; t < 4 && slot == ~0u; ++t) {
+                        const uint32_t m = *(volatile uint32_t*) mask;
+                        if (m == ~0u) break;
+                        const uint32_t bit = __ffs(~m) - 1;
+                        if (!(atomicOr(mask, 1u << bit) & (1u << bit))) slot = bit;
+                    }
+                slot = __shfl_sync(0xffffffffu, slot, 0);
+                if (slot != ~0u) {
+                    if (lane == wl) {
+                        if (fl & kAFollow) {
+                            // the walk stands on Gamma_j's trajectory: inside
+                            // region j its G-pass record, at the next region's
+                            // first block Gamma_j's walk record there
+                            const uint2 r0 = (jb % p.nb == 0 && jb / p.nb >= jk + 2)
+                                                 ? __ldcg(p.rec_w + (size_t) jb * p.dmax)
+                                                 : __ldcg(p.rec_g + jb);
+                            a_rec = r0.x;
+                            ca += r0.y;
+                        }
+                        if (kCap && cl.on) {   // the seeded walk does not capture
+                            cap_flush(cl, slice, ca, p.cap_bytes, true);
+                            p.cap_valid[jk] = cl.on ? ca : cl.done;
+                            cl.on = false;
+                        }
+                    }
+                    seeded_walk<kCap>(p, tb, tile, bar, win, timed_out, wl,
+                                      __shfl_sync(0xffffffffu, jk, wl), jb, a_rec, ca,
+                                      p.seed_ring + ((size_t) slot * 32 + lane) * kSeedRing);
+                    if (lane == 0) {
+                        atomicAnd(mask, ~(1u << slot));
+                        atomicAdd(p.scan_flags + ntile + 5, 1u);   // seeded walks (statistics)
+                    }
+                    open = false;
+                    break;   // the warp's last walk has ended
+                }
+            }
+        }
         // stage units [jb * B, jb * B + kWindowUnits + 4) of every open lane
         const uint32_t u0 = jb * B;
         const uint32_t avail = (open && u0 < n) ? min(tile_units, n - u0) : 0u;
@@ -679,8 +1033,7 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
             const uint32_t d = reg - jk;
             if (d > p.dmax) {
                 atomicOr(p.status, MANS_DEV_SYNC_OVERFLOW);
-                p.m[jk] = ~0ull;
-                p.delta[jk] = 0;
+                publish_merge(p, jk, ~0ull, 0);
                 open = false;
                 break;
             }
@@ -714,8 +1067,8 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
             }
             p.rec_w[(size_t) b * p.dmax + (d - 1)] = make_uint2(ax, cab);
             if (ax == gx) {
-                p.m[jk] = (uint64_t) b * Bbits + (ax & 0xffu);
-                p.delta[jk] = (long long) cab - (long long) cgb;
+                publish_merge(p, jk, (uint64_t) b * Bbits + (ax & 0xffu),
+                              (long long) cab - (long long) cgb);
                 open = false;
                 break;
             }
@@ -781,8 +1134,7 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
             rg = rg_next;
             if (jb == reg_end) { ++reg; reg_end += p.nb; }
             if (jb >= p.nblk) {
-                p.m[jk] = ~0ull;   // no merge before the stream end
-                p.delta[jk] = 0;
+                publish_merge(p, jk, ~0ull, 0);   // no merge before the stream end
                 open = false;
             }
             // the capture covers region k + 1 only
@@ -800,6 +1152,7 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
         if (open) {
             if (!(fl & kAFollow)) a_rec = (A.pos - bs) | (entry_index(A.a, tb) << 8);
             if (g_rec != ~0u && !(fl & kGFollow)) g_rec = (G.pos - bs) | (entry_index(G.a, tb) << 8);
+            ++wins;
         }
     }
     __syncwarp();
@@ -808,7 +1161,7 @@ __device__ __forceinline__ void wwalk_body(const DecodeParams& p) {
 }
 
 template <bool kCap>
-__global__ void __launch_bounds__(kWalkThreads) k_wwalk(DecodeParams p) { wwalk_body<kCap>(p); }
+__global__ void __launch_bounds__(kWalkThreads) k_wwalk(DecodeParams p) { wwalk_body<kCap, true>(p); }
 
 // Tiles are taken in launch order through an atomic ticket (the word after
 // the flags), so a tile only waits on tiles that have already started.
@@ -1597,8 +1950,8 @@ __global__ void __launch_bounds__(kWalkThreads) k_wwalk_batch(const DecodeParams
         const uint32_t it = s_item;
         if (it >= total) return;
         load_params(sp, ps + list[it]);
-        if (sp.cap_bytes) wwalk_body<true>(sp);
-        else wwalk_body<false>(sp);
+        if (sp.cap_bytes) wwalk_body<true, false>(sp);
+        else wwalk_body<false, false>(sp);
         __syncthreads();   // sp and s_item are rewritten next
     }
 }
@@ -1654,7 +2007,7 @@ __global__ void __launch_bounds__(kFinalThreads) k_final_batch(const DecodeParam
 
 struct AuxLayout {
     size_t rec_g, rec_w, m, delta, Mpre, Dpre, status, tab_sync, tab_sym, scan_tiles,
-        scan_flags, walk_jobs, cap_valid, fb_list, cap, total;
+        scan_flags, walk_jobs, cap_valid, fb_list, cap, seed_ring, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t) 255; }
@@ -1749,7 +2102,10 @@ static void set_kernel_attributes() {
     if (dev < 64) done |= 1ull << dev;
 }
 
-static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax, size_t cap_bytes) {
+// seeds: room for the seeded walks' records (plain decodes; batches run
+// without seeds)
+static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax, size_t cap_bytes,
+                            bool seeds = true) {
     AuxLayout a;
     size_t o = 0;
     a.status = o; o += 256;
@@ -1763,12 +2119,14 @@ static AuxLayout layout_for(size_t nblk, size_t nreg, size_t dmax, size_t cap_by
     a.Dpre = o; o += align256(nreg * 8);
     const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
     a.scan_tiles = o; o += align256(ntiles * sizeof(ScanTile));
-    // flags, ticket, job count, next job, fallback warp count
-    a.scan_flags = o; o += align256((ntiles + 4) * 4);
+    // flags, ticket, job count, next job, fallback warp count, seed slots,
+    // seeded walks
+    a.scan_flags = o; o += align256((ntiles + 6) * 4);
     a.walk_jobs = o; o += align256(nreg * sizeof(WJob));
     a.cap_valid = o; o += cap_bytes ? align256(nreg * 4) : 0;
     a.fb_list = o; o += cap_bytes ? align256((nblk + 31) / 32 * 4) : 0;
     a.cap = o; o += cap_bytes ? align256(nreg * cap_bytes + 16) : 0;
+    a.seed_ring = o; o += seeds ? align256((size_t) kSeedSlots * 32 * kSeedRing * sizeof(uint2)) : 0;
     a.total = o;
     return a;
 }
@@ -1846,6 +2204,15 @@ static double mean_meeting_units(uint32_t L, double bits_per_symbol) {
 constexpr double kCaptureMinBits = 2.0;
 constexpr uint32_t kCaptureMaxL = 4096;   // larger tables leave too little shared memory
 constexpr size_t kCaptureMinUnits = 16u << 20;
+// Seeded walks from 1 to 4.5 bits per symbol, to 7 bits at L >= 4096
+// (measured at 256 MiB, seeds on against off: L = 1024 at 3.8 bits per
+// symbol +7.7 %, 1.5 bits +2.2 %; L = 4096 at 6.0 bits +3.2 %, 1.5 bits
+// +6.5 %; at 8.6 and 0.67 bits, and 6.0 bits with L = 1024, 0.4-1.5 %
+// slower: their walks are short, and the rest of their seeds fall on the
+// next region's trajectory)
+constexpr double kSeedMinBits = 1.0;
+constexpr double kSeedMaxBits = 4.5;
+constexpr double kSeedMaxBitsLarge = 7.0;   // L >= 4096
 
 // The planner's choices a measured table entry overrides (see
 // mans_tune_table.h): units per block, the shortest region in mean meeting
@@ -1930,6 +2297,10 @@ static int plan_core(size_t n_units, size_t n_out, uint32_t L, const mans_cfg* h
     // a table plan without capture says so, so that the plan given back as
     // a hint (its geometry fixed) keeps deciding the same way
     if (kn && !capture) c.flags |= MANS_DECODE_NO_CAPTURE;
+    // seeded walks where walks are long
+    if (!(c.flags & (MANS_DECODE_SEEDS | MANS_DECODE_NO_SEEDS)) && bps >= kSeedMinBits &&
+        bps < (L >= 4096 ? kSeedMaxBitsLarge : kSeedMaxBits))
+        c.flags |= MANS_DECODE_SEEDS;
     *out = c;
     return MANS_OK;
 }
@@ -2152,11 +2523,13 @@ static int decode_impl(const uint32_t* d_units, size_t n_units, uint8_t* d_out,
     p.cap = cfg.capture_bytes ? (uint8_t*) (base + lay.cap) : nullptr;
     p.cap_valid = cfg.capture_bytes ? (uint32_t*) (base + lay.cap_valid) : nullptr;
     p.fb_list = cfg.capture_bytes ? (uint32_t*) (base + lay.fb_list) : nullptr;
+    p.seed_ring = (cfg.flags & MANS_DECODE_SEEDS) && !(cfg.flags & MANS_DECODE_NO_SEEDS)
+                      ? (uint2*) (base + lay.seed_ring) : nullptr;
     const bool capture = cfg.capture_bytes != 0;
 
     const size_t ntiles = (nreg + kScanTile - 1) / kScanTile;
     if (cudaMemsetAsync(p.status, 0, sizeof(uint32_t), st) != cudaSuccess ||
-        cudaMemsetAsync(base + lay.scan_flags, 0, (ntiles + 4) * 4, st) != cudaSuccess)
+        cudaMemsetAsync(base + lay.scan_flags, 0, (ntiles + 6) * 4, st) != cudaSuccess)
         return MANS_ERR_CUDA;
     const size_t smem = ((size_t) L * sizeof(uint2) + 15) & ~(size_t) 15;
     set_kernel_attributes();
@@ -2386,7 +2759,7 @@ int mans_sync_stats_get(const void* d_aux, size_t aux_bytes, size_t n_units, siz
     // flags (flags, ticket, job count, next job, fallback warp count): all
     // inside the workspace whose size was checked above
     std::vector<unsigned long long> m(nreg);
-    uint32_t cnt[4] = {0, 0, 0, 0};
+    uint32_t cnt[6] = {0, 0, 0, 0, 0, 0};
     cudaStream_t st = (cudaStream_t) stream;
     const char* base = (const char*) d_aux;
     if (cudaMemcpyAsync(m.data(), base + lay.m, nreg * 8, cudaMemcpyDeviceToHost, st) !=
@@ -2404,6 +2777,7 @@ int mans_sync_stats_get(const void* d_aux, size_t aux_bytes, size_t n_units, siz
     s.walks = nreg > 0 ? nreg - 1 : 0;
     s.open_walks = cnt[1];
     s.fallback_warps = cfg.capture_bytes ? cnt[3] : 0;
+    s.seeded_walks = cnt[5];
     uint64_t walk_bits = 0;
     for (size_t k = 0; k + 1 < nreg; ++k) {
         // region k's walk starts at the first bit of region k + 1 and ends
@@ -2576,7 +2950,7 @@ struct BatchLayout {
 };
 
 static size_t stream_data_bytes(const BatchStreamPlan& sp) {
-    const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots, sp.cfg.capture_bytes);
+    const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots, sp.cfg.capture_bytes, false);
     return a.total;
 }
 
@@ -2776,7 +3150,7 @@ int batch_create(const mans_stream_desc* streams, uint32_t n, const mans_cfg* hi
         p.status = (uint32_t*) (b->base + b->lay.status) + i;
         if (!sp.active) continue;
         const mans_stream_desc& d = streams[i];
-        const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots, sp.cfg.capture_bytes);
+        const AuxLayout a = layout_for(sp.nblk, sp.nreg, sp.cfg.walk_slots, sp.cfg.capture_bytes, false);
         char* slice = slices ? (char*) slices[i] : b->base + b->lay.data + sp.data_off;
         if (!slice || ((uintptr_t) slice & 255) != 0) { mans_batch_destroy(b); return MANS_ERR_ARG; }
         b->slice[i] = slice;
