@@ -64,50 +64,88 @@ __device__ __forceinline__ void scan_body(const P& p, uint32_t tile) {
         if (t >= off) { s_m[t] = max(s_m[t], xm); s_s[t] += xs; }
         __syncthreads();
     }
+    // the tile's aggregate, then its exclusive prefix by a warp-wide look-back:
+    // lane l reads tile j - l, so one round trip covers 32 predecessors
+    // (their aggregates up to the nearest inclusive prefix)
+    __shared__ unsigned long long s_am;
+    __shared__ long long s_as;
     if (t == kScanThreads - 1) {
-        const unsigned long long am = s_m[t];
-        const long long as = s_s[t];
+        s_am = s_m[t];
+        s_as = s_s[t];
+    }
+    __syncthreads();
+    if (t < 32) {
+        const unsigned long long am = s_am;
+        const long long as = s_as;
         unsigned long long pm = 0;
         long long ps = 0;
         if (tile == 0) {
-            tiles[0].inc_m = am;
-            tiles[0].inc_s = as;
-            __threadfence();
-            atomicExch(flags + 0, 2u);
+            if (t == 0) {
+                tiles[0].inc_m = am;
+                tiles[0].inc_s = as;
+                __threadfence();
+                atomicExch(flags + 0, 2u);
+            }
         } else {
-            tiles[tile].agg_m = am;
-            tiles[tile].agg_s = as;
-            __threadfence();
-            atomicExch(flags + tile, 1u);
-            // look back
+            if (t == 0) {
+                tiles[tile].agg_m = am;
+                tiles[tile].agg_s = as;
+                __threadfence();
+                atomicExch(flags + tile, 1u);
+            }
             int32_t j = (int32_t) tile - 1;
             uint32_t spins = 0;
             while (j >= 0) {
-                const uint32_t f = *(volatile uint32_t*) (flags + j);
-                if (f == 0) {
-                    if (++spins > (1u << 24)) {
-                        atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
+                const int32_t q = j - (int32_t) t;
+                uint32_t f = 0;
+                unsigned long long vm = 0;
+                long long vs = 0;
+                if (q >= 0) {
+                    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(f) : "l"(flags + q) : "memory");
+                    if (f == 2) {
+                        vm = *(volatile unsigned long long*) &tiles[q].inc_m;
+                        vs = *(volatile long long*) &tiles[q].inc_s;
+                    } else if (f == 1) {
+                        vm = *(volatile unsigned long long*) &tiles[q].agg_m;
+                        vs = *(volatile long long*) &tiles[q].agg_s;
+                    }
+                }
+                // lanes 0 .. stop: the predecessors down to the nearest
+                // inclusive prefix (tile 0's always is one)
+                const uint32_t incl = __ballot_sync(0xffffffffu, q >= 0 && f == 2);
+                const uint32_t stop = incl ? __ffs(incl) - 1 : 31u;
+                const uint32_t upto = stop == 31 ? 0xffffffffu : ((2u << stop) - 1u);
+                const uint32_t valid = __ballot_sync(0xffffffffu, q >= 0);
+                if (__ballot_sync(0xffffffffu, q >= 0 && f == 0) & upto & valid) {
+                    if (++spins > (1u << 24)) {   // a predecessor never published
+                        if (t == 0) atomicOr(p.status, MANS_DEV_SCAN_TIMEOUT);
                         break;
                     }
                     continue;
                 }
-                __threadfence();
-                if (f == 2) {
-                    pm = max(pm, *(volatile unsigned long long*) &tiles[j].inc_m);
-                    ps += *(volatile long long*) &tiles[j].inc_s;
-                    break;
+                unsigned long long wm = t <= stop ? vm : 0ull;
+                long long ws = t <= stop ? vs : 0ll;
+#pragma unroll
+                for (uint32_t o = 16; o; o >>= 1) {
+                    wm = max(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+                    ws += __shfl_xor_sync(0xffffffffu, ws, o);
                 }
-                pm = max(pm, *(volatile unsigned long long*) &tiles[j].agg_m);
-                ps += *(volatile long long*) &tiles[j].agg_s;
-                --j;
+                pm = max(pm, wm);
+                ps += ws;
+                if (incl) break;
+                j -= 32;
             }
-            tiles[tile].inc_m = max(pm, am);
-            tiles[tile].inc_s = ps + as;
-            __threadfence();
-            atomicExch(flags + tile, 2u);
+            if (t == 0) {
+                tiles[tile].inc_m = max(pm, am);
+                tiles[tile].inc_s = ps + as;
+                __threadfence();
+                atomicExch(flags + tile, 2u);
+            }
         }
-        s_pm = pm;
-        s_ps = ps;
+        if (t == 0) {
+            s_pm = pm;
+            s_ps = ps;
+        }
     }
     __syncthreads();
     unsigned long long run_m = max(s_pm, t ? s_m[t - 1] : 0ull);
