@@ -215,7 +215,9 @@ def measure_batched(args, ws, rank, local):
             return t0.elapsed_time(t1) / nsteps, (nsteps - 1) & 1
 
         run(2)
-        runs = [run(6) for _ in range(3)]   # median: the host links are shared
+        # the bench's own K steps (the pipeline fills and drains once per
+        # run); median of three: the host links are shared
+        runs = [run(max(6, args.steps)) for _ in range(3)]
         e2e_ms = sorted(r[0] for r in runs)[1]
         last = runs[-1][1]
         acc2, _ = sets[last][3].status(stream)
