@@ -367,7 +367,11 @@ int mans_decode_loop(const mans_stream_desc* streams, uint32_t n, const mans_cfg
  * output, decode workspace) fits the range, copies host inputs in on a copy
  * stream, and launches everything admitted since the previous launch as one
  * batch on a free stream; host outputs are copied back behind the batch on
- * the same stream.  A request whose memory could never fit is completed
+ * the same stream.  Small requests (n_out <= small_bytes) have one more
+ * stream of their own, at the device's highest stream priority: they are
+ * batched there, apart from the larger requests, so that a small request
+ * does not wait for a batch of large ones to decode and copy back.  A
+ * request whose memory could never fit is completed
  * with MANS_ERR_NOMEM; bad arguments with MANS_ERR_ARG.
  * mans_server_poll returns completions (waiting up to wait_us for one).
  * Host buffers should be page-locked (cudaHostAlloc / cudaHostRegister):
@@ -379,7 +383,10 @@ typedef struct {
     uint64_t budget_bytes;    /* device memory the server may hold; 0 = 16 GiB */
     uint32_t max_inflight;    /* batches on the GPU at once; 0 = 2 */
     uint32_t max_batch;       /* requests per launch; 0 = 4096 */
-    uint32_t reserved[2];
+    uint32_t small_bytes;     /* requests with n_out at most this are batched on
+                                 the small-request stream; 0 = 1 MiB,
+                                 UINT32_MAX = no small-request stream */
+    uint32_t reserved;
 } mans_server_cfg;
 
 #define MANS_REQ_DEVICE_IO 0x1u     /* units / out are caller-owned device memory */

@@ -13,7 +13,9 @@
 //                           ready ──(H2D of inputs on the copy stream)
 //                              │ a launch slot is free
 //                              ▼
-//            one batch = everything ready, on the slot's stream:
+//            one batch = everything ready of the slot's size class, on
+//            the slot's stream (small requests have a slot of their own,
+//            on a high-priority stream):
 //            wait(copies) → upload params → 4 batch kernels → D2H outputs
 //                              │ host callback at the end of the stream work
 //                              ▼
@@ -47,6 +49,8 @@ namespace {
 constexpr uint64_t kDefaultBudget = 16ull << 30;
 constexpr uint64_t kHeadroom = 1ull << 30;      // left to other users of the device
 constexpr uint64_t kHeaderCap = 8ull << 20;     // preallocated header per slot
+constexpr uint64_t kSmallHeaderCap = 1ull << 20;   // ... of the small-request slot
+constexpr uint32_t kDefaultSmall = 1u << 20;    // small request: n_out <= 1 MiB
 constexpr uint64_t kNone = ~0ull;
 
 uint64_t clock_ns() {
@@ -90,6 +94,7 @@ struct Req {
     bool checked = false;
     int check_rc = 0;
     bool host_in = false, host_out = false, pinned_out = false;
+    bool taken = false;            // chosen for the batch being built
     mans_stream_desc d{};
     char* slice = nullptr;
 };
@@ -98,6 +103,8 @@ struct Slot {
     cudaStream_t stream = nullptr;
     uint64_t header_off = kNone;   // preallocated header
     uint64_t extra_off = kNone;    // larger header for this batch, if needed
+    uint64_t header_cap = kHeaderCap;
+    bool small = false;            // takes small requests only
     mans_batch* b = nullptr;
     std::vector<Req*> reqs;
     uint64_t seq = 0;
@@ -111,6 +118,7 @@ struct Slot {
 struct mans_server {
     int device = 0;
     uint32_t max_inflight = 2, max_batch = 4096;
+    uint64_t small_bytes = 0;      // 0: no small-request slot
     char* base = nullptr;
     mans::Arena arena;
     std::mutex arena_mu;
@@ -151,8 +159,12 @@ struct mans_server {
         return MANS_OK;
     }
 
-    cudaStream_t copy_stream = nullptr;
-    cudaEvent_t copy_ev = nullptr;
+    // input copies, one in-order stream per size class (a small request's
+    // copy does not queue behind a large one's), and the event a batch of
+    // that class waits on
+    cudaStream_t copy_stream[2] = {nullptr, nullptr};
+    cudaEvent_t copy_ev[2] = {nullptr, nullptr};
+    int size_class(const Req* q) const { return small_bytes && q->r.n_out <= small_bytes; }
     std::vector<std::unique_ptr<Slot>> slots;
 
     // mailbox + worker wake-up
@@ -312,7 +324,8 @@ struct mans_server {
                 q->d.d_units = (const uint32_t*) p;
                 p += align256(q->r.n_units * 4);
                 if (cudaMemcpyAsync((void*) q->d.d_units, q->r.units, q->r.n_units * 4,
-                                    cudaMemcpyHostToDevice, copy_stream) != cudaSuccess) {
+                                    cudaMemcpyHostToDevice, copy_stream[size_class(q)]) !=
+                    cudaSuccess) {
                     cudaGetLastError();
                     complete(q, MANS_ERR_CUDA, 0, 0);
                     progress = true;
@@ -336,30 +349,48 @@ struct mans_server {
         s->srv->cv.notify_all();
     }
 
-    // Launches everything ready (up to max_batch) on a free slot.
+    // Takes q out of the ready queue and completes it with rc.
+    void drop_ready(Req* q, int rc) {
+        ready.erase(std::find(ready.begin(), ready.end(), q));
+        complete(q, rc, 0, 0);
+    }
+
+    // Launches one batch on a free slot, in arrival order, up to max_batch
+    // requests: the small-request slot (offered first) takes the small
+    // requests that are ready; any other slot the larger ones, or, when none
+    // is ready, the small ones the busy small-request slot has left.
     bool launch() {
         if (ready.empty()) return false;
         Slot* s = nullptr;
-        for (auto& c : slots)
-            if (!c->busy) { s = c.get(); break; }
+        std::vector<Req*> take;
+        for (auto& c : slots) {
+            if (c->busy) continue;
+            for (int want = c->small; want <= 1 && take.empty(); ++want)
+                for (Req* q : ready) {
+                    if (take.size() >= max_batch) break;
+                    if (size_class(q) == want) take.push_back(q);
+                }
+            if (!take.empty()) {
+                s = c.get();
+                break;
+            }
+        }
         if (!s) return false;
-        size_t n = std::min<size_t>(ready.size(), max_batch);
+        size_t n = take.size();
         std::vector<mans_stream_desc> descs(n);
         std::vector<void*> slices(n);
         size_t hbytes = 0;
         uint64_t hoff = s->header_off;
         for (;;) {
             for (size_t i = 0; i < n; ++i) {
-                descs[i] = ready[i]->d;
-                slices[i] = ready[i]->slice;
+                descs[i] = take[i]->d;
+                slices[i] = take[i]->slice;
             }
             if (mans_batch_header_size(descs.data(), (uint32_t) n, nullptr, &hbytes) != MANS_OK) {
-                Req* q = ready.front();   // cannot happen for validated requests
-                ready.pop_front();
-                complete(q, MANS_ERR_ARG, 0, 0);
+                drop_ready(take[0], MANS_ERR_ARG);   // cannot happen for validated requests
                 return true;
             }
-            if (hbytes <= kHeaderCap) break;
+            if (hbytes <= s->header_cap) break;
             if (n > 1) { n = (n + 1) / 2; continue; }
             uint64_t off;
             bool ok;
@@ -369,21 +400,21 @@ struct mans_server {
             }
             if (ok) { s->extra_off = hoff = off; break; }
             if (any_busy()) return false;   // wait for memory to come back
-            Req* q = ready.front();
-            ready.pop_front();
-            complete(q, MANS_ERR_NOMEM, 0, 0);
+            drop_ready(take[0], MANS_ERR_NOMEM);
             return true;
         }
-        // the copy stream is in order: one event covers every input copied so far
-        cudaEventRecord(copy_ev, copy_stream);
-        cudaStreamWaitEvent(s->stream, copy_ev, 0);
+        // a copy stream is in order: one event covers every input of the
+        // taken requests' size class (they are all of one) copied so far
+        const int cls = size_class(take[0]);
+        cudaEventRecord(copy_ev[cls], copy_stream[cls]);
+        cudaStreamWaitEvent(s->stream, copy_ev[cls], 0);
         mans_batch* b = nullptr;
         int rc = mans_batch_create_split(descs.data(), (uint32_t) n, nullptr, base + hoff,
                                          hbytes, slices.data(), s->stream, &b);
         if (rc == MANS_OK) rc = mans_batch_decode(b, s->stream);
         if (rc == MANS_OK) {
             for (size_t i = 0; i < n; ++i) {
-                Req* q = ready[i];
+                Req* q = take[i];
                 if (q->pinned_out &&
                     cudaMemcpyAsync(q->r.out, q->d.d_out, q->r.n_out, cudaMemcpyDeviceToHost,
                                     s->stream) != cudaSuccess) {
@@ -392,8 +423,10 @@ struct mans_server {
                 }
             }
         }
-        s->reqs.assign(ready.begin(), ready.begin() + n);
-        ready.erase(ready.begin(), ready.begin() + n);
+        s->reqs.assign(take.begin(), take.begin() + n);
+        for (size_t i = 0; i < n; ++i) take[i]->taken = true;
+        ready.erase(std::remove_if(ready.begin(), ready.end(), [](const Req* q) { return q->taken; }),
+                    ready.end());
         s->b = b;
         s->seq = ++next_seq;
         s->done.store(false);
@@ -499,7 +532,7 @@ struct mans_server {
         lk.unlock();
         // requests admitted but not launched may still have input copies in
         // flight from the caller's memory: let them end before returning
-        cudaStreamSynchronize(copy_stream);
+        for (cudaStream_t cs : copy_stream) cudaStreamSynchronize(cs);
         for (Req* q : pending) delete q;
         for (Req* q : ready) delete q;
         pending.clear();
@@ -520,13 +553,15 @@ int mans_server_create(const mans_server_cfg* cfg, mans_server** out) {
     if (cudaGetDevice(&s->device) != cudaSuccess) return MANS_ERR_CUDA;
     s->max_inflight = c.max_inflight ? std::min<uint32_t>(c.max_inflight, 8) : 2;
     s->max_batch = c.max_batch ? std::min<uint32_t>(c.max_batch, 1u << 20) : 4096;
+    s->small_bytes = c.small_bytes == 0xffffffffu ? 0 : (c.small_bytes ? c.small_bytes : kDefaultSmall);
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return MANS_ERR_CUDA;
     uint64_t budget = c.budget_bytes ? c.budget_bytes : kDefaultBudget;
     if (free_b > kHeadroom) budget = std::min<uint64_t>(budget, free_b - kHeadroom);
     else budget = 0;
     budget &= ~255ull;
-    const uint64_t headers = (uint64_t) s->max_inflight * kHeaderCap;
+    const uint64_t headers =
+        (uint64_t) s->max_inflight * kHeaderCap + (s->small_bytes ? kSmallHeaderCap : 0);
     if (budget < headers + (1ull << 20)) return MANS_ERR_NOMEM;
     if (cudaMalloc(&s->base, budget) != cudaSuccess) {
         cudaGetLastError();
@@ -536,20 +571,31 @@ int mans_server_create(const mans_server_cfg* cfg, mans_server** out) {
     auto fail = [&](int rc) {
         for (auto& sl : s->slots)
             if (sl->stream) cudaStreamDestroy(sl->stream);
-        if (s->copy_ev) cudaEventDestroy(s->copy_ev);
-        if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+        for (int i = 0; i < 2; ++i) {
+            if (s->copy_ev[i]) cudaEventDestroy(s->copy_ev[i]);
+            if (s->copy_stream[i]) cudaStreamDestroy(s->copy_stream[i]);
+        }
         cudaFree(s->base);
         return rc;
     };
-    if (cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&s->copy_ev, cudaEventDisableTiming) != cudaSuccess)
-        return fail(MANS_ERR_CUDA);
-    for (uint32_t i = 0; i < s->max_inflight; ++i) {
+    for (int i = 0; i < 2; ++i)
+        if (cudaStreamCreateWithFlags(&s->copy_stream[i], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&s->copy_ev[i], cudaEventDisableTiming) != cudaSuccess)
+            return fail(MANS_ERR_CUDA);
+    // the small-request slot first (it is offered the ready requests first),
+    // on a stream of the highest priority: its blocks are scheduled ahead of
+    // the waiting blocks of the larger batches' kernels
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) return fail(MANS_ERR_CUDA);
+    for (uint32_t i = s->small_bytes ? 0 : 1; i <= s->max_inflight; ++i) {
         auto sl = std::make_unique<Slot>();
         sl->srv = s.get();
-        if (cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) != cudaSuccess)
+        sl->small = i == 0;
+        sl->header_cap = sl->small ? kSmallHeaderCap : kHeaderCap;
+        if (cudaStreamCreateWithPriority(&sl->stream, cudaStreamNonBlocking,
+                                         sl->small ? greatest : least) != cudaSuccess)
             return fail(MANS_ERR_CUDA);
-        if (!s->arena.alloc(kHeaderCap, &sl->header_off)) return fail(MANS_ERR_NOMEM);
+        if (!s->arena.alloc(sl->header_cap, &sl->header_off)) return fail(MANS_ERR_NOMEM);
         s->slots.push_back(std::move(sl));
     }
     s->st.range_bytes = budget;
@@ -629,8 +675,10 @@ int mans_server_destroy(mans_server* s) {
     for (Req* q : s->mailbox) delete q;
     for (auto& sl : s->slots)
         if (sl->stream) cudaStreamDestroy(sl->stream);
-    if (s->copy_ev) cudaEventDestroy(s->copy_ev);
-    if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
+    for (int i = 0; i < 2; ++i) {
+        if (s->copy_ev[i]) cudaEventDestroy(s->copy_ev[i]);
+        if (s->copy_stream[i]) cudaStreamDestroy(s->copy_stream[i]);
+    }
     if (s->base) cudaFree(s->base);
     delete s;
     return MANS_OK;

@@ -22,11 +22,13 @@ REQ_DEVICE_IO = 0x1
 REQ_SOURCE_ORDER = 0x2
 REQ_CONTAINER = 0x4
 REQ_NO_CAPTURE = 0x8
+SMALL_OFF = 0xFFFFFFFF   # ServerCfg.small_bytes: no small-request stream
 
 
 class ServerCfg(ctypes.Structure):
     _fields_ = [("budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_uint32),
-                ("max_batch", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
+                ("max_batch", ctypes.c_uint32), ("small_bytes", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class RequestC(ctypes.Structure):
@@ -127,9 +129,10 @@ def request_container(container, out, tag=0, arrival_ns=0, source_order=False) -
 
 
 class Server:
-    def __init__(self, budget_bytes: int = 0, max_inflight: int = 0, max_batch: int = 0):
+    def __init__(self, budget_bytes: int = 0, max_inflight: int = 0, max_batch: int = 0,
+                 small_bytes: int = 0):
         self._L = _sig()
-        cfg = ServerCfg(int(budget_bytes), int(max_inflight), int(max_batch))
+        cfg = ServerCfg(int(budget_bytes), int(max_inflight), int(max_batch), int(small_bytes))
         h = ctypes.c_void_p(0)
         check(self._L.mans_server_create(ctypes.byref(cfg), ctypes.byref(h)), "mans_server_create")
         self._h = h

@@ -159,7 +159,8 @@ def measure(args, ws, rank, local):
     h_out = [torch.empty(max(1, st.n), dtype=torch.uint8).pin_memory() for st in sts]
 
     inflight = int(os.environ.get("MANS_SERVE_INFLIGHT", "0"))   # 0: the library default
-    srv = serve.Server(budget_bytes=budget, max_inflight=inflight)
+    small = int(os.environ.get("MANS_SERVE_SMALL", "0"))         # 0: the library default
+    srv = serve.Server(budget_bytes=budget, max_inflight=inflight, small_bytes=small)
     tids = [srv.add_table(st.table) for st in sts]
     cap = not getattr(args, "no_capture", False)
     rp_dev = Replay(serve, entry, [t.data_ptr() for t in d_units], [t.data_ptr() for t in d_out],
@@ -288,7 +289,8 @@ def measure(args, ws, rank, local):
         "e2e": {"value": round(ws * total_sym / e2e_s / 1e9, 3), "unit": "GB/s",
                 "h2d_bytes_per_step": total_comp, "d2h_bytes_per_step": total_sym},
         "gpu_launches": int(round((s1["kernel_launches"] - s0["kernel_launches"]) / steps)),
-        "server": {"batches_per_step": round(batches, 1), "largest_batch": stats["largest_batch"],
+        "server": {"small_request_bytes": (0 if small == serve.SMALL_OFF else (small or 1 << 20)),
+                   "batches_per_step": round(batches, 1), "largest_batch": stats["largest_batch"],
                    "admission_waits": stats["admission_waits"], "range_peak": stats["range_peak"],
                    "streams_redone": stats["streams_redone"], "failed": stats["failed"]},
         "clocks": clk.summary(),

@@ -123,6 +123,46 @@ def test_staggered_arrivals_join_later_launches(mg):
         assert srv.stats()["batches"] >= 2
 
 
+def test_small_requests_batched_apart(mg):
+    """Requests of at most small_bytes output go to the small-request slot's
+    batches, larger ones to the other slots: submitted together, the two
+    classes share no launch; without the small-request slot they share one.
+    Requests of one class only still use every slot."""
+    from multians_gb300 import serve
+    rng = np.random.default_rng(23)
+    from multians_gb300 import host
+    small = [host.make_stream(2300 + i, float(rng.uniform(0.01, 1.0)), int(rng.integers(2_000, 200_000)),
+                              1024) for i in range(8)]
+    large = [host.make_stream(2400 + i, float(rng.uniform(0.01, 1.0)), int(rng.integers(1_200_000, 2_500_000)),
+                              1024 if i % 2 else 4096) for i in range(4)]
+    threshold = 1 << 20
+    for small_bytes, apart in ((threshold, True), (serve.SMALL_OFF, False)):
+        with serve.Server(budget_bytes=1 << 30, small_bytes=small_bytes) as srv:
+            items = _setup(srv, small + large)
+            for it in items:
+                it[3].fill_(0xCD)
+            srv.submit([_req(serve, it, i) for i, it in enumerate(items)])
+            done = {c.tag: c for c in srv.wait(len(items))}
+            assert all(c.status == 0 for c in done.values()), done
+            for st, _, _, out in items:
+                assert np.array_equal(out.numpy()[::-1], st.symbols)
+            sb = {done[i].batch for i in range(len(small))}
+            lb = {done[i].batch for i in range(len(small), len(items))}
+            if apart:
+                assert sb.isdisjoint(lb), (sb, lb)
+                assert len(sb) == 1 and len(lb) == 1   # one launch per class
+            else:
+                assert sb == lb and len(sb) == 1
+            # small requests only, arriving while a batch of them runs: the
+            # other slots take them too
+            srv.submit([_req(serve, items[i], 100 + i) for i in range(len(small))])
+            srv.submit([_req(serve, items[i], 200 + i) for i in range(len(small))])
+            again = srv.wait(2 * len(small))
+            assert all(c.status == 0 for c in again), again
+            for st, _, _, out in items[: len(small)]:
+                assert np.array_equal(out.numpy()[::-1], st.symbols)
+
+
 def test_device_io_pageable_and_errors(mg):
     import torch
 
