@@ -129,6 +129,11 @@ def request_container(container, out, tag=0, arrival_ns=0, source_order=False) -
 
 
 class Server:
+    """mans_server_create's settings: device range (0 = 16 GiB), batches in
+    flight (0 = 2), requests per launch (0 = 4096) and the small-request
+    threshold in decoded bytes (0 = 1 MiB; SMALL_OFF: no separate slot for
+    small requests)."""
+
     def __init__(self, budget_bytes: int = 0, max_inflight: int = 0, max_batch: int = 0,
                  small_bytes: int = 0):
         self._L = _sig()
