@@ -361,7 +361,8 @@ int mans_decode_loop(const mans_stream_desc* streams, uint32_t n, const mans_cfg
  * blocking call on the default stream (include/cuhd_gpu_decoder.h:22-36).
  * A server owns one device range of budget_bytes (default 16 GiB, capped at
  * creation by the free device memory less 1 GiB), a worker thread and
- * max_inflight CUDA streams.  Tables are added once and stay resident.
+ * max_inflight CUDA streams (one more for small requests, below).  Tables
+ * are added once and stay resident.
  * mans_server_submit queues requests and returns at once.  The worker admits
  * queued requests in arrival order while each one's device memory (units,
  * output, decode workspace) fits the range, copies host inputs in on a copy
@@ -381,7 +382,8 @@ typedef struct mans_server mans_server;
 
 typedef struct {
     uint64_t budget_bytes;    /* device memory the server may hold; 0 = 16 GiB */
-    uint32_t max_inflight;    /* batches on the GPU at once; 0 = 2 */
+    uint32_t max_inflight;    /* batches on the GPU at once, besides the
+                                 small-request stream's; 0 = 2 */
     uint32_t max_batch;       /* requests per launch; 0 = 4096 */
     uint32_t small_bytes;     /* requests with n_out at most this are batched on
                                  the small-request stream; 0 = 1 MiB,
