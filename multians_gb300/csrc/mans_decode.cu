@@ -333,7 +333,10 @@ __device__ __forceinline__ void cap_flush(CapLane& cl, uint8_t* __restrict__ dst
 // the merge-walk pass (k_wwalk).  The cap trades the G pass's lane
 // efficiency (a warp waits for its longest walk) against the merge-walk
 // pass's load; measured at 256 MiB, 6 bits per symbol: 32 units 356 GB/s,
-// 64 units 370, 128 units 363.
+// 64 units 370, 128 units 363; measured again with the current passes, 48
+// and 96 units against 64: 369-375 and 371-373 GB/s against 375-378, the
+// G pass 0.365 and 0.387 ms against 0.373, the walks 0.188 and 0.167-0.169
+// against 0.175.
 constexpr uint32_t kWalkCapUnits = 64;
 template <bool kCap>
 __device__ __forceinline__ void gwalk_body(const DecodeParams& p, uint32_t rbase) {
@@ -569,7 +572,7 @@ __global__ void __launch_bounds__(kSyncThreadsMax) k_gwalk(DecodeParams p) {
 // ring is primed with the partial group the G pass wrote.
 constexpr uint32_t kWalkThreads = 64;
 constexpr uint32_t kWalkCtasMax = 152 * 8;
-constexpr uint32_t kWindowUnits = 128;
+constexpr uint32_t kWindowUnits = 128;   // 256 measured slower (fewer CTAs per SM)
 constexpr uint32_t kWindowTile = (kWindowUnits + 4) * 4;     // bytes per lane
 constexpr uint32_t kWindowStride = kWindowTile;   // 132 words: 8 bank groups, 16-byte aligned
 
