@@ -277,6 +277,11 @@ __device__ __forceinline__ uint32_t cap_row(uint32_t col, uint32_t c) {
 template <bool kAligned>
 __device__ __forceinline__ uint32_t cap_run(SCursor& A, const UnitSrc& src, CapLane& cl,
                                             uint32_t cs, uint32_t be) {
+    // unrolled by four (a test before every step): measured at 256 MiB
+    // against no unrolling, 375-377 -> 378-380 GB/s at lambda = 0.05,
+    // 234-236 -> 240-242 at lambda = 0.2 (G pass and walks both faster),
+    // 422 -> 424 at lambda = 0.005; by two: in between
+#pragma unroll 4
     while (A.pos < be) {
         cl.acc = __byte_perm(cl.acc, A.step(src), 0x7321);
         sts32(kAligned ? (cl.col | (cs & 0xF80u)) : cl.col + (cs & 0xF80u), cl.acc);

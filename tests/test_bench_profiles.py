@@ -13,7 +13,7 @@ def test_profile_figures_by_kernel_and_capture_mode():
     kernel_of, traffic, issue, inst = bench.profile_figures(wl, True)
     assert kernel_of["k_final"] == "k_copy<0>"
     # dram read + write of each kernel in the committed captures
-    assert traffic == {"k_gwalk<1>": 631_873_024, "k_wwalk<1>": 46_875_648,
+    assert traffic == {"k_gwalk<1>": 631_123_968, "k_wwalk<1>": 46_963_712,
                        "k_copy<0>": 594_449_920}
     assert set(issue) == set(inst) == {"k_gwalk<1>", "k_wwalk<1>", "k_copy<0>"}
     assert all(0 < v <= 100 for v in issue.values())
